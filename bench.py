@@ -1,0 +1,398 @@
+"""Benchmark of the KD-tree KNN query on one GB300.
+
+Workload (default): large single-cloud query, d=3, float32 -- 4,194,304
+reference points (half uniform cube, half noisy unit sphere), 1,048,576
+queries uniform in [-0.1, 1.1]^3, k = 16.  A step is one exact KNN query of
+all queries.  "plain" = the reference's default tree depth and the default
+launch shape; "chosen" = autotuned depth and lanes per query, replayed as a
+captured CUDA graph.  `value` is the chosen queries/s with inputs resident in
+HBM; `e2e` goes through the public API with host buffers.
+
+    python bench.py [--steps K] [--warmup W] [--impl ours|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "KNN queries/s (d=3,k=16,4M ref) chosen vs plain on 1 GB300 at exact indices"
+UNIT = "queries/s"
+K_NN = 16
+WORKLOAD = ("large single-cloud KD query: 4,194,304 refs (half U[0,1]^3, half unit sphere at (0.5,0.5,0.5) "
+            "with N(0,0.01) radial noise), 1,048,576 queries U[-0.1,1.1]^3, k=16, float32")
+L2_FLUSH_BYTES = 512 << 20
+
+
+def env_int(name, default):
+    try:
+        return int(os.environ.get(name, default))
+    except ValueError:
+        return default
+
+
+# ------------------------------------------------------------ clocks --
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, ValueError):
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if self.proc is None or not self.path or not os.path.exists(self.path):
+            return None
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ------------------------------------------------------------ helpers --
+
+def measured_peak_hbm():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, ValueError, KeyError):
+        return 6800.0, "fallback"
+
+
+def profiled_traffic(kernel_tag: str):
+    """DRAM bytes per launch of a kernel from its committed ncu summary
+    (profiles/<kernel_tag>.md, line 'traffic_bytes_per_launch: <int>'), or None."""
+    path = os.path.join(ROOT, "profiles", kernel_tag + ".md")
+    try:
+        m = re.search(r"traffic_bytes_per_launch:\s*([0-9]+)", open(path).read())
+        return int(m.group(1)) if m else None
+    except OSError:
+        return None
+
+
+def algorithmic_bytes(n_ref, nq, k, levels, d=3):
+    """Bytes a KD query launch must move at minimum: queries in (4d per query),
+    results out (8k per query), and the tree once: point records (16 B each),
+    split values (4 B each) and leaf offsets (4 B each)."""
+    return nq * (4 * d + 8 * k) + 16 * n_ref + 4 * ((1 << levels) - 1) + 4 * ((1 << levels) + 1)
+
+
+# -------------------------------------------------------- reference arm --
+
+def run_reference(args):
+    """The reference's CPU query path timed on this host's cores: the
+    reference's own sources (oracle/_ref) where they were built, else the
+    oracle's C restatement of them."""
+    from oracle import oracle as O
+    from torch_kdtree_gb300.synthetic import cube_and_sphere
+    O.build()
+    ref, q = cube_and_sphere()
+    threads = os.cpu_count() or 1
+    kind = "port"
+    if O.ref_available():
+        try:
+            O.ref_lib()
+            kind = "reference"
+        except OSError:
+            kind = "port"
+    sample = min(len(q), args.ref_sample)
+    qs = q[:sample]
+    t0 = time.perf_counter()
+    if kind == "reference":
+        os.environ["OMP_NUM_THREADS"] = str(threads)
+        tree = O.RefTree(ref, O.default_levels(len(ref)))
+    else:
+        lay = O.build_tree(ref, O.default_levels(len(ref)), nthreads=threads)
+    build_s = time.perf_counter() - t0
+    times = []
+    for step in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        if kind == "reference":
+            tree.query(qs, K_NN, local=True)
+        else:
+            O.query_tree(lay, qs, K_NN, nthreads=threads, local=True)
+        dt = time.perf_counter() - t0
+        if step >= args.warmup:
+            times.append(dt)
+    total = sum(times)
+    value = sample * len(times) / total
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / len(times),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded numpy, shapes and distributions of the workload)",
+        "config": {"workload": WORKLOAD, "levels": O.default_levels(len(ref)),
+                   "sample_queries_per_step": sample, "tree_build_s": build_s},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind,
+                         "sample": f"first {sample} of the 1,048,576 queries per step, full 4,194,304-point tree"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------- our arm --
+
+def run_ours(args, rank, world):
+    import torch
+
+    import torch_kdtree_gb300 as tk
+    from torch_kdtree_gb300._lib import QueryOpts
+    from torch_kdtree_gb300.autotune import autotune
+    from torch_kdtree_gb300.nn_distance import knn_query_raw
+    from torch_kdtree_gb300.synthetic import cube_and_sphere
+
+    dev = torch.device("cuda", env_int("LOCAL_RANK", 0))
+    torch.cuda.set_device(dev)
+    ref_np, q_np = cube_and_sphere(seed=0)
+    if rank:  # replicas: same cloud, own queries
+        _, q_np = cube_and_sphere(seed=1000 + rank)
+    n_ref, nq = ref_np.shape[0], q_np.shape[0]
+    ref = torch.from_numpy(ref_np).to(dev)
+    q = torch.from_numpy(q_np).to(dev)
+
+    # ---- plain: reference heuristic depth, default launch shape
+    t0 = time.perf_counter()
+    plain = tk.build_kd_tree(ref)
+    build_plain_s = time.perf_counter() - t0
+    # ---- chosen: autotuned depth and lanes per query
+    t0 = time.perf_counter()
+    ch = autotune(ref, q, K_NN, use_cache=False)
+    tune_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    chosen = tk.build_kd_tree(ref, levels=ch.levels, query_opts=QueryOpts.make(threads_per_query=ch.threads_per_query))
+    build_chosen_s = time.perf_counter() - t0
+
+    d_plain = torch.empty(nq, K_NN, device=dev)
+    i_plain = torch.empty(nq, K_NN, dtype=torch.int32, device=dev)
+    d_ch = torch.empty_like(d_plain)
+    i_ch = torch.empty_like(i_plain)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+
+    # chosen step as one captured graph (binning + KD kernel, no host work)
+    s = torch.cuda.Stream(dev)
+    s.wait_stream(torch.cuda.current_stream(dev))
+    with torch.cuda.stream(s):
+        knn_query_raw(chosen._tree, q, K_NN, d_ch, i_ch, chosen.query_opts)
+    torch.cuda.current_stream(dev).wait_stream(s)
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        knn_query_raw(chosen._tree, q, K_NN, d_ch, i_ch, chosen.query_opts)
+
+    def step_chosen():
+        graph.replay()
+
+    def step_plain():
+        knn_query_raw(plain._tree, q, K_NN, d_plain, i_plain, plain.query_opts)
+
+    def timed(fn, steps, warmup):
+        for _ in range(warmup):
+            flush.zero_()
+            fn()
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        ms = []
+        for _ in range(steps):
+            flush.zero_()
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record()
+            fn()
+            b.record()
+            b.synchronize()
+            ms.append(a.elapsed_time(b))
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        return ms
+
+    with ClockSampler(dev.index) as clk:
+        ms_chosen = timed(step_chosen, args.steps, args.warmup)
+        ms_plain = timed(step_plain, args.steps, args.warmup)
+    clocks = clk.summary()
+
+    same = bool(torch.equal(i_plain, i_ch) and torch.equal(d_plain, d_ch))
+
+    # ---- dominant kernel alone (events recorded inside the library around the KD kernel)
+    ks = torch.cuda.Event(enable_timing=True)
+    ke = torch.cuda.Event(enable_timing=True)
+    ks.record()
+    ke.record()  # materialise the events
+    torch.cuda.synchronize()
+    kopts = QueryOpts.make(threads_per_query=ch.threads_per_query, kernel_start_event=ks.cuda_event,
+                           kernel_stop_event=ke.cuda_event)
+    kern_ms = []
+    for _ in range(max(3, args.steps)):
+        flush.zero_()
+        knn_query_raw(chosen._tree, q, K_NN, d_ch, i_ch, kopts)
+        ke.synchronize()
+        kern_ms.append(ks.elapsed_time(ke))
+    kern_avg = sum(kern_ms) / len(kern_ms)
+
+    # ---- end to end through the public API, host buffers in and out
+    q_host = torch.from_numpy(q_np).pin_memory()
+    d_host = torch.empty(nq, K_NN).pin_memory()
+    i_host = torch.empty(nq, K_NN, dtype=torch.int32).pin_memory()
+
+    def step_e2e():
+        dd, ii = chosen.query(q_host, nr_nns_searches=K_NN)
+        d_host.copy_(dd, non_blocking=True)
+        i_host.copy_(ii, non_blocking=True)
+
+    ms_e2e = timed(step_e2e, args.steps, args.warmup)
+
+    # max over ranks
+    def world_max(v):
+        if world == 1:
+            return v
+        t = torch.tensor([v], dtype=torch.float64, device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        return float(t.item())
+
+    t_chosen = world_max(sum(ms_chosen))
+    t_plain = world_max(sum(ms_plain))
+    t_e2e = world_max(sum(ms_e2e))
+    if rank != 0:
+        return
+
+    value = world * nq * args.steps / (t_chosen / 1e3)
+    plain_value = world * nq * args.steps / (t_plain / 1e3)
+    peak, peak_kind = measured_peak_hbm()
+    alg = algorithmic_bytes(n_ref, nq, K_NN, ch.levels)
+    achieved = alg / (kern_avg / 1e3) / 1e9
+    traffic = profiled_traffic("kd_query_cube_sphere_4M_k16")
+
+    # ---- CPU baseline (oracle / reference CPU path) on a bounded sample, plus an exactness check of that sample
+    cpu = None
+    exact = None
+    if not args.no_cpu_baseline:
+        cpu, exact = cpu_baseline(ref_np, q_np, i_ch[: args.ref_sample].cpu().numpy(),
+                                  d_ch[: args.ref_sample].cpu().numpy(), args.ref_sample)
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_chosen / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded numpy, shapes and distributions of the workload)",
+        "config": {"workload": WORKLOAD, "levels": ch.levels, "threads_per_query": ch.threads_per_query,
+                   "graph_captured": True, "l2": f"flushed between steps ({L2_FLUSH_BYTES >> 20} MiB write)",
+                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                   "tree_build_s": {"plain": build_plain_s, "chosen": build_chosen_s}, "autotune_s": tune_s},
+        "plain": {"value": plain_value, "ms_per_step": t_plain / args.steps, "levels": plain.levels,
+                  "threads_per_query": "auto"},
+        "chosen_vs_plain": value / plain_value,
+        "identical_results_plain_vs_chosen": same,
+        "autotune_table": [list(map(lambda x: round(x, 4) if isinstance(x, float) else x, r)) for r in ch.table],
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_kind": peak_kind, "traffic": traffic, "kernel": "k_kd_query",
+                     "kernel_ms": kern_avg, "algorithmic_bytes_per_launch": alg},
+        "cpu_baseline": cpu,
+        "exactness_vs_oracle_sample": exact,
+        "e2e": {"value": world * nq * args.steps / (t_e2e / 1e3), "unit": UNIT,
+                "h2d_bytes_per_step": q_host.numel() * 4,
+                "d2h_bytes_per_step": d_host.numel() * 4 + i_host.numel() * 4,
+                "ms_per_step": t_e2e / args.steps},
+        "gpu_launches": 4 * args.steps,
+        "clocks": clocks,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def cpu_baseline(ref_np, q_np, gpu_idx, gpu_d, sample):
+    """The oracle's restatement of the reference CPU query, timed on the host
+    cores on the first `sample` queries; also checks the GPU's answers for
+    that sample against it (distances bitwise, indices up to exact ties)."""
+    from oracle import oracle as O
+    O.build()
+    threads = os.cpu_count() or 1
+    L = O.default_levels(len(ref_np))
+    lay = O.build_tree(ref_np, L, nthreads=threads)
+    qs = q_np[:sample]
+    t0 = time.perf_counter()
+    od, oi = O.query_tree(lay, qs, K_NN, nthreads=threads)
+    dt = time.perf_counter() - t0
+    cmp = O.compare_knn(od, oi, gpu_d, gpu_idx)
+    cpu = {"value": sample / dt, "unit": UNIT, "cores": threads, "kind": "port",
+           "sample": f"first {sample} of the 1,048,576 queries, full 4,194,304-point tree (levels {L})"}
+    exact = {"queries": sample, "index_mismatches_non_tie": cmp.mismatches, "tie_queries": cmp.tie_queries,
+             "dist_bit_mismatches": cmp.dist_bit_mismatch}
+    return cpu, exact
+
+
+def main():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--ref-sample", type=int, default=131072)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    args = p.parse_args()
+    args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
+    world = env_int("WORLD_SIZE", 1)
+    rank = env_int("RANK", 0)
+    if args.impl == "reference":
+        if rank == 0:
+            run_reference(args)
+        return
+    if world > 1:
+        import torch
+        torch.distributed.init_process_group("nccl")
+    run_ours(args, rank, world)
+    if world > 1:
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

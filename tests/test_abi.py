@@ -1,0 +1,135 @@
+"""The C ABI without a GPU: the library loads, exports every function that
+include/*.h declares, and its host tree builder reproduces the reference's
+layout (fixtures made by the reference itself)."""
+import ctypes
+import glob
+import os
+import re
+
+import numpy as np
+import pytest
+
+from golden_util import inputs_of
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    names = []
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        src = open(h).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        names += re.findall(r"^\s*(?:const\s+)?[A-Za-z_][A-Za-z0-9_]*\s*\**\s+\**(tk_[a-z0-9_]+)\s*\(", src, re.M)
+    return sorted(set(names))
+
+
+def test_header_declares_the_boundary():
+    names = declared_functions()
+    for must in ("tk_tree_create", "tk_tree_query", "tk_tree_destroy", "tk_tree_get_perm", "tk_tree_get_points",
+                 "tk_knn_backward", "tk_last_error"):
+        assert must in names
+
+
+def test_library_exports_every_declared_symbol():
+    from torch_kdtree_gb300 import _lib
+    lib = ctypes.CDLL(_lib.LIB_PATH)
+    missing = [n for n in declared_functions() if not hasattr(lib, n)]
+    assert not missing, missing
+    # and the Python binding declares a signature for each of them
+    assert not [n for n in declared_functions() if n not in _lib.SIGNATURES]
+
+
+def host_tree(points, levels):
+    from torch_kdtree_gb300._lib import LIB, TkError, check  # noqa: F401
+    h = ctypes.c_void_p()
+    dt = 0 if points.dtype == np.float32 else 1
+    st = LIB.tk_tree_create(points.ctypes.data, points.shape[0], points.shape[1], dt, levels, -1, 0,
+                            ctypes.byref(h))
+    return st, h
+
+
+def layout_of(h, n, d, levels, dtype):
+    from torch_kdtree_gb300._lib import LIB, check
+    perm = np.empty(n, np.int32)
+    pts = np.empty((n, d), dtype)
+    med = np.empty((1 << levels) - 1, dtype)
+    off = np.empty((1 << levels) + 1, np.int32)
+    check(LIB.tk_tree_get_perm(h, perm.ctypes.data))
+    check(LIB.tk_tree_get_points(h, pts.ctypes.data))
+    check(LIB.tk_tree_get_splits(h, med.ctypes.data, off.ctypes.data))
+    return pts, perm, med, off
+
+
+@pytest.mark.parametrize("name", [
+    "grid_f32_d1_n1000_q200_k10", "grid_f32_d2_n10000_q300_k20", "grid_f32_d3_n10000_q300_k20",
+    "grid_f64_d1_n10000_q300_k20", "grid_f64_d3_n1000_q200_k10", "grid_f32_d3_n30_q20_k5",
+    "grid_f64_d2_n5_q5_k1", "levels_f32_d3_n1000_L9", "levels_f32_d3_n1000_L1"])
+def test_host_build_matches_reference_layout(name, golden):
+    from torch_kdtree_gb300._lib import LIB, check
+    case = golden[name]
+    ref, _ = inputs_of(case)
+    n, d = ref.shape
+    L = int(case["levels"])
+    st, h = host_tree(ref, L)
+    check(st)
+    try:
+        pts, perm, med, off = layout_of(h, n, d, L, ref.dtype)
+    finally:
+        LIB.tk_tree_destroy(h)
+    np.testing.assert_array_equal(pts, case["structured"])
+    np.testing.assert_array_equal(perm, case["perm"])
+    np.testing.assert_array_equal(med, case["medians"])
+    depth = np.floor(np.log2(np.arange(len(med)) + 1)).astype(int)
+    np.testing.assert_array_equal(depth % d, case["axes"])
+    np.testing.assert_array_equal(off[:-1], case["leaf_off"])
+    np.testing.assert_array_equal(np.diff(off), case["leaf_cnt"])
+
+
+def test_host_build_matches_oracle_on_large_cloud(oracle):
+    """Selection-based build == the oracle's full-sort build at 200k points."""
+    from torch_kdtree_gb300._lib import LIB, check
+    rng = np.random.default_rng(5)
+    ref = rng.random((200_000, 3)).astype(np.float32)
+    lay = oracle.build_tree(ref, 13)
+    st, h = host_tree(ref, 13)
+    check(st)
+    try:
+        pts, perm, med, off = layout_of(h, 200_000, 3, 13, np.float32)
+    finally:
+        LIB.tk_tree_destroy(h)
+    np.testing.assert_array_equal(pts, lay.structured)
+    np.testing.assert_array_equal(perm, lay.perm)
+    np.testing.assert_array_equal(med, lay.medians)
+
+
+def test_error_paths_without_gpu():
+    from torch_kdtree_gb300._lib import LIB, TK_EINVAL
+    rng = np.random.default_rng(3)
+    pts = rng.standard_normal((10, 3)).astype(np.float32)
+    st, _ = host_tree(pts, 6)  # 32 split nodes for 10 points
+    assert st == TK_EINVAL and "Ran out of points" in LIB.tk_last_error().decode()
+    st, _ = host_tree(pts, 0)
+    assert st == TK_EINVAL
+    st, _ = host_tree(pts, 25)
+    assert st == TK_EINVAL
+    bad = pts.copy()
+    bad[3, 1] = np.nan
+    st, _ = host_tree(bad, 2)
+    assert st == TK_EINVAL and "NaN" in LIB.tk_last_error().decode()
+    four_d = rng.standard_normal((10, 4)).astype(np.float32)
+    st, _ = host_tree(four_d, 2)
+    assert st == TK_EINVAL
+    # a host-only tree refuses queries instead of computing anything on the CPU
+    st, h = host_tree(pts, 2)
+    assert st == 0
+    d = np.empty((1, 1), np.float32)
+    i = np.empty((1, 1), np.int32)
+    st = LIB.tk_tree_query(h, pts.ctypes.data, 1, 1, d.ctypes.data, i.ctypes.data, None, None, 0, None)
+    assert st == TK_EINVAL
+    LIB.tk_tree_destroy(h)
+
+
+def test_default_levels_matches_reference_heuristic():
+    from torch_kdtree_gb300 import default_levels
+    for n, L in [(5, 1), (30, 1), (1000, 6), (100_000, 13), (4_194_304, 13), (16, 1), (128, 4)]:
+        assert default_levels(n) == L

@@ -1,0 +1,103 @@
+"""The hand-written backward (tk_knn_backward) against the reference's
+torch-indexed gradient, FP64 central finite differences, and itself
+(bitwise determinism)."""
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+cuda = torch.device("cuda")
+
+
+def tk():
+    import torch_kdtree_gb300
+    return torch_kdtree_gb300
+
+
+def torch_indexed_grads(q, ref, inds, w):
+    """The reference's gradient path: re-gather and autograd through indexing
+    (torch_kdtree/nn_distance.py:111-112)."""
+    q = q.detach().clone().requires_grad_(True)
+    ref = ref.detach().clone().requires_grad_(True)
+    d = torch.sum((q[:, None] - ref[inds.long()]) ** 2, dim=-1)
+    (0.5 * (d * w).sum()).backward()
+    return q.grad, ref.grad
+
+
+@pytest.mark.parametrize("dtype,tol", [(torch.float32, 1e-5), (torch.float64, 1e-12)])
+@pytest.mark.parametrize("d", [1, 2, 3])
+def test_matches_torch_indexed_gradient(dtype, tol, d):
+    g = torch.Generator(device="cpu").manual_seed(7)
+    ref = torch.randn(20000, d, generator=g, dtype=dtype).to(cuda).requires_grad_(True)
+    q = torch.randn(30000, d, generator=g, dtype=dtype).to(cuda).requires_grad_(True)
+    k = 8
+    w = torch.rand(30000, k, generator=g, dtype=dtype).to(cuda)
+    tree = tk().build_kd_tree(ref)
+    dists, inds = tree.query(q, nr_nns_searches=k)
+    (0.5 * (dists * w).sum()).backward()
+    gq_t, gr_t = torch_indexed_grads(q, ref, inds, w)
+    scale_q = gq_t.abs().max().item()
+    scale_r = gr_t.abs().max().item()
+    assert (q.grad - gq_t).abs().max().item() <= tol * scale_q * 10
+    assert (ref.grad - gr_t).abs().max().item() <= tol * scale_r * 10
+
+
+def test_backward_is_bitwise_deterministic():
+    g = torch.Generator(device="cpu").manual_seed(8)
+    ref = torch.randn(100000, 3, generator=g).to(cuda)
+    q = torch.randn(100000, 3, generator=g).to(cuda)
+    w = torch.rand(100000, 8, generator=g).to(cuda)
+    outs = []
+    for _ in range(3):
+        r = ref.clone().requires_grad_(True)
+        qq = q.clone().requires_grad_(True)
+        dists, _ = tk().build_kd_tree(r).query(qq, nr_nns_searches=8)
+        (0.5 * (dists * w).sum()).backward()
+        outs.append((qq.grad.clone(), r.grad.clone()))
+    for a, b in outs[1:]:
+        assert torch.equal(a[0], outs[0][0])
+        assert torch.equal(a[1], outs[0][1])
+
+
+def test_finite_differences_fp64():
+    """Central differences (step 1e-4, FP64) of loss = 0.5 * sum(dists * w)
+    with the neighbour lists held fixed, on a 4,096-point subset."""
+    g = torch.Generator(device="cpu").manual_seed(9)
+    n = 200_000
+    ref = torch.randn(n, 3, generator=g).to(cuda).requires_grad_(True)
+    q = torch.randn(n, 3, generator=g).to(cuda).requires_grad_(True)
+    w = torch.rand(n, 8, generator=g).to(cuda)
+    dists, inds = tk().build_kd_tree(ref).query(q, nr_nns_searches=8)
+    (0.5 * (dists * w).sum()).backward()
+
+    q64 = q.detach().double()
+    r64 = ref.detach().double()
+    w64 = w.double()
+    il = inds.long()
+
+    def loss(qv, rv):
+        return 0.5 * (torch.sum((qv[:, None] - rv[il]) ** 2, -1) * w64).sum()
+
+    h = 1e-4
+    sub = torch.randperm(n, generator=g)[:4096].to(cuda)
+    # query coordinates: perturb one coordinate of all subset points at once
+    # (their loss terms are independent), per axis
+    for c in range(3):
+        e = torch.zeros_like(q64)
+        e[sub, c] = h
+        # per-point contributions: only rows in sub change
+        lp = 0.5 * (torch.sum(((q64 + e)[sub][:, None] - r64[il[sub]]) ** 2, -1) * w64[sub]).sum(1)
+        lm = 0.5 * (torch.sum(((q64 - e)[sub][:, None] - r64[il[sub]]) ** 2, -1) * w64[sub]).sum(1)
+        fd = (lp - lm) / (2 * h)
+        an = q.grad[sub, c].double()
+        rel = ((an - fd).abs() / fd.abs().clamp_min(1e-2)).max().item()
+        assert rel < 1e-3, rel
+    # reference coordinates: one point at a time for a smaller subset
+    for m in sub[:64].tolist():
+        for c in range(3):
+            e = torch.zeros_like(r64)
+            e[m, c] = h
+            fd = ((loss(q64, r64 + e) - loss(q64, r64 - e)) / (2 * h)).item()
+            an = ref.grad[m, c].item()
+            assert abs(an - fd) <= 1e-3 * max(abs(fd), 1e-3), (m, c, an, fd)

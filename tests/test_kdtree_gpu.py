@@ -1,0 +1,178 @@
+"""GPU parity of the KD-tree query (through the C ABI via the Python API).
+
+Bar: bit-exact against the oracle's exhaustive search ordered by
+(distance, original index); against the reference's own outputs (golden
+fixtures), distances bitwise and indices equal except inside exact ties."""
+import numpy as np
+import pytest
+import torch
+
+from golden_util import inputs_of, rows
+from make_golden import CASES
+
+pytestmark = pytest.mark.gpu
+
+cuda = torch.device("cuda")
+
+
+def tk():
+    import torch_kdtree_gb300
+    return torch_kdtree_gb300
+
+
+def gpu_query(ref, q, k, levels=None, **opts):
+    from torch_kdtree_gb300._lib import QueryOpts
+    qo = QueryOpts.make(**opts) if opts else None
+    tree = tk().build_kd_tree(torch.from_numpy(ref).to(cuda), levels=levels, query_opts=qo)
+    d, i = tree.query(torch.from_numpy(q).to(cuda), nr_nns_searches=k)
+    torch.cuda.synchronize()
+    return d.cpu().numpy(), i.cpu().numpy()
+
+
+@pytest.mark.parametrize("name", [c[0] for c in CASES])
+def test_golden_fixtures(name, golden, oracle):
+    case = golden[name]
+    ref, q = inputs_of(case)
+    k = int(case["k"])
+    d, i = gpu_query(ref, q, k, levels=int(case["levels"]))
+    # canonical answer: bit-exact
+    bd, bi = oracle.brute(ref, q, k)
+    np.testing.assert_array_equal(d, bd)
+    np.testing.assert_array_equal(i, bi)
+    # the reference's own answer: equal up to exact-distance ties
+    r = rows(case)
+    cmp = oracle.compare_knn(case["dists"], case["idx"], d[:r], i[:r])
+    assert cmp.ok, cmp
+
+
+@pytest.mark.parametrize("tpq", [1, 2, 4, 8, 16, 32])
+@pytest.mark.parametrize("k", [1, 5, 16, 33, 128])
+def test_launch_shapes_give_identical_results(tpq, k, oracle):
+    rng = np.random.default_rng(11)
+    ref = rng.standard_normal((20000, 3)).astype(np.float32)
+    q = (rng.standard_normal((3000, 3)) * 1.2).astype(np.float32)
+    bd, bi = oracle.brute(ref, q, k)
+    for binq in (0, 1):
+        d, i = gpu_query(ref, q, k, levels=9, threads_per_query=tpq, bin_queries=binq)
+        np.testing.assert_array_equal(d, bd)
+        np.testing.assert_array_equal(i, bi)
+
+
+@pytest.mark.parametrize("levels", [1, 2, 3, 7, 11, 13, 14])
+def test_any_tree_depth_gives_identical_results(levels, oracle):
+    rng = np.random.default_rng(12)
+    ref = rng.random((20000, 3)).astype(np.float32)
+    q = (rng.random((2500, 3)) * 1.2 - 0.1).astype(np.float32)
+    bd, bi = oracle.brute(ref, q, 16)
+    for smem in (0, 5, 12):
+        d, i = gpu_query(ref, q, 16, levels=levels, smem_levels=smem)
+        np.testing.assert_array_equal(d, bd)
+        np.testing.assert_array_equal(i, bi)
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+@pytest.mark.parametrize("d", [1, 2, 3])
+def test_reference_test_grid(dtype, d, oracle):
+    """The grid of the reference's test_kdtree (tests/test_knn_unit.py:30-70):
+    refs x queries x k, N(0,1)*1e3 data, k > N must raise."""
+    rng = np.random.default_rng(100 + d)
+    for nr_refs in (5, 10, 20, 30, 1000, 10000):
+        ref = (rng.standard_normal((nr_refs, d)) * 1e3).astype(dtype)
+        tree = tk().build_kd_tree(torch.from_numpy(ref).to(cuda))
+        for nr_query in (5, 10, 20, 30, 1000):
+            q = (rng.standard_normal((nr_query, d)) * 1e3).astype(dtype)
+            qt = torch.from_numpy(q).to(cuda)
+            for k in (1, 5, 10, 20):
+                if k > nr_refs:
+                    with pytest.raises(Exception):
+                        tree.query(qt, nr_nns_searches=k)
+                    continue
+                dists, inds = tree.query(qt, nr_nns_searches=k)
+                assert dists.device.type == "cuda" and inds.device.type == "cuda"
+                assert inds.shape == (nr_query, k) and dists.shape == (nr_query, k)
+                bd, bi = oracle.brute(ref, q, k)
+                np.testing.assert_array_equal(dists.cpu().numpy(), bd)
+                np.testing.assert_array_equal(inds.cpu().numpy(), bi)
+
+
+def test_duplicate_points_ties_break_by_lower_index(oracle):
+    rng = np.random.default_rng(13)
+    base = rng.standard_normal((500, 3)).astype(np.float32)
+    ref = np.concatenate([base, base, base[:100]])  # exact duplicates, later copies have higher indices
+    q = base[:200] + np.float32(1e-3)
+    d, i = gpu_query(ref, q, 6)
+    bd, bi = oracle.brute(ref, q, 6)
+    np.testing.assert_array_equal(i, bi)
+    np.testing.assert_array_equal(d, bd)
+    # each query sees its source point twice (or three times) at equal distance: lower index first
+    assert np.all(i[:, 0] < i[:, 1])
+
+
+def test_api_errors():
+    t = tk()
+    pts = torch.randn(10, 3, device=cuda)
+    tree = t.build_kd_tree(pts)
+    with pytest.raises(Exception):
+        tree.query(torch.randn(10, 3, dtype=torch.float64, device=cuda))  # wrong dtype
+    with pytest.raises(Exception):
+        tree.query(torch.randn(5, 3, device=cuda), nr_nns_searches=11)  # k > N
+    with pytest.raises(Exception):
+        t.build_kd_tree(np.random.uniform(size=(10, 436)), device="cuda")  # uncompiled dimension
+    with pytest.raises(Exception):
+        t.build_kd_tree(torch.randn(10, 3), device="cpu")  # this engine builds CUDA trees only
+
+
+def test_empty_query_and_result_buffers(oracle):
+    rng = np.random.default_rng(14)
+    ref = rng.standard_normal((1000, 3)).astype(np.float32)
+    tree = tk().build_kd_tree(torch.from_numpy(ref).to(cuda))
+    d, i = tree.query(torch.empty(0, 3, device=cuda), nr_nns_searches=4)
+    assert d.shape == (0, 4) and i.shape == (0, 4)
+    q = rng.standard_normal((64, 3)).astype(np.float32)
+    rd = torch.empty(64, 4, device=cuda)
+    ri = torch.empty(64, 4, dtype=torch.int32, device=cuda)
+    d, i = tree.query(torch.from_numpy(q), nr_nns_searches=4, result_dists=rd, result_idx=ri)  # host query
+    assert d.data_ptr() == rd.data_ptr() and i.data_ptr() == ri.data_ptr()
+    bd, bi = oracle.brute(ref, q, 4)
+    np.testing.assert_array_equal(rd.cpu().numpy(), bd)
+    np.testing.assert_array_equal(ri.cpu().numpy(), bi)
+
+
+def test_sqrt_distances():
+    pts = torch.randn(2000, 3, device=cuda)
+    q = torch.randn(100, 3, device=cuda)
+    d2, i2 = tk().build_kd_tree(pts).query(q, nr_nns_searches=3)
+    d1, i1 = tk().build_kd_tree(pts, squared_distances=False).query(q, nr_nns_searches=3)
+    assert torch.equal(i1, i2)
+    assert torch.equal(d1, torch.sqrt(d2))
+
+
+@pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
+def test_grad_like_reference(dtype):
+    """tests/test_knn_unit.py:90-107 of the reference."""
+    dims = 3
+    points_ref = torch.randn(size=(10, dims), dtype=dtype, device=cuda, requires_grad=True)
+    t_kdtree = tk().build_kd_tree(points_ref)
+    points_query = torch.randn(size=(5, dims), dtype=dtype, device=cuda, requires_grad=True)
+    dists, inds = t_kdtree.query(points_query, nr_nns_searches=2)
+    (0.5 * torch.sum(dists)).backward()
+    assert points_query.grad is not None
+    assert torch.allclose(points_query.grad, torch.sum((points_query[:, None] - points_ref[inds.long()]), axis=-2))
+    assert points_ref.grad is not None
+    points_ref_grad = torch.zeros_like(points_ref)
+    for i, ind in enumerate(inds.long()):
+        points_ref_grad[ind] += points_ref[ind] - points_query[i]
+    assert torch.allclose(points_ref.grad, points_ref_grad)
+
+
+def test_nan_query_row_is_isolated(oracle):
+    rng = np.random.default_rng(15)
+    ref = rng.standard_normal((5000, 3)).astype(np.float32)
+    q = rng.standard_normal((300, 3)).astype(np.float32)
+    q[17, 1] = np.nan
+    d, i = gpu_query(ref, q, 4)
+    ok = np.ones(300, bool)
+    ok[17] = False
+    bd, bi = oracle.brute(ref, q[ok], 4)
+    np.testing.assert_array_equal(d[ok], bd)
+    np.testing.assert_array_equal(i[ok], bi)

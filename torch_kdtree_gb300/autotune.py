@@ -1,0 +1,118 @@
+"""Autotuner for the KD query launch: tree depth (leaf size) and lanes per query.
+
+For a given reference cloud, a query sample and k, it builds the tree at a
+few depths around the reference's heuristic, times every lanes-per-query
+shape with CUDA events, and keeps the fastest.  Results do not depend on the
+choice (the search is exact with a shape-independent tie rule), only speed
+does.  Choices are cached in a JSON file keyed by (n, query count bucket, k,
+dims, dtype, GPU name).
+"""
+from __future__ import annotations
+
+import json
+import math
+import os
+from dataclasses import asdict, dataclass
+from typing import Optional, Sequence
+
+import torch
+
+from ._lib import QueryOpts
+from .nn_distance import TorchKDTree, build_kd_tree, default_levels, knn_query_raw
+
+CACHE_PATH = os.environ.get("TK_AUTOTUNE_CACHE",
+                            os.path.join(os.path.expanduser("~"), ".cache", "torch_kdtree_gb300", "autotune.json"))
+LANES = (1, 2, 4, 8, 16, 32)
+
+
+@dataclass
+class Choice:
+    levels: int
+    threads_per_query: int
+    ms: float
+    plain_levels: int
+    table: list  # (levels, lanes, ms) of every timed candidate
+
+
+def _key(n, nq, k, d, dtype, device) -> str:
+    name = torch.cuda.get_device_name(device)
+    return f"{name}|n={n}|q~2^{int(round(math.log2(max(nq, 1))))}|k={k}|d={d}|{dtype}"
+
+
+def _load_cache() -> dict:
+    try:
+        with open(CACHE_PATH) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def _store_cache(c: dict) -> None:
+    try:
+        os.makedirs(os.path.dirname(CACHE_PATH), exist_ok=True)
+        with open(CACHE_PATH, "w") as f:
+            json.dump(c, f, indent=1)
+    except OSError:
+        pass
+
+
+def time_query(tree: TorchKDTree, q: torch.Tensor, k: int, opts: QueryOpts, reps: int = 3) -> float:
+    """Median milliseconds of one tk_tree_query (binning + KD kernel)."""
+    d = torch.empty(q.shape[0], k, dtype=tree.dtype, device=q.device)
+    i = torch.empty(q.shape[0], k, dtype=torch.int32, device=q.device)
+    knn_query_raw(tree._tree, q, k, d, i, opts)  # warm-up
+    times = []
+    for _ in range(reps):
+        s = torch.cuda.Event(enable_timing=True)
+        e = torch.cuda.Event(enable_timing=True)
+        s.record()
+        knn_query_raw(tree._tree, q, k, d, i, opts)
+        e.record()
+        e.synchronize()
+        times.append(s.elapsed_time(e))
+    times.sort()
+    return times[len(times) // 2]
+
+
+def autotune(points_ref: torch.Tensor, queries: torch.Tensor, k: int,
+             levels_candidates: Optional[Sequence[int]] = None, lanes: Sequence[int] = LANES,
+             reps: int = 3, use_cache: bool = True, max_queries: int = 1 << 20) -> Choice:
+    """Pick (levels, threads_per_query) for querying ``points_ref`` with
+    queries like ``queries`` (a sample of at most ``max_queries`` is timed)."""
+    n, d = points_ref.shape
+    key = _key(n, queries.shape[0], k, d, str(points_ref.dtype), points_ref.device)
+    cache = _load_cache() if use_cache else {}
+    if use_cache and key in cache:
+        return Choice(**cache[key])
+    L0 = default_levels(n)
+    if levels_candidates is None:
+        # deepest useful tree keeps >= ~4 points per leaf
+        lmax = max(1, min(24, int(math.log2(max(n, 2))) - 2))
+        levels_candidates = sorted({max(1, min(lmax, L)) for L in range(L0 - 1, L0 + 7)})
+    q = queries[:max_queries].contiguous()
+    table = []
+    best = None
+    for L in levels_candidates:
+        try:
+            tree = build_kd_tree(points_ref, levels=L)
+        except Exception:  # too deep for this cloud
+            continue
+        for g in lanes:
+            if g * 16 < k:  # a lane holds at most 16 list entries
+                continue
+            ms = time_query(tree, q, k, QueryOpts.make(threads_per_query=g), reps)
+            table.append((L, g, ms))
+            if best is None or ms < best[2]:
+                best = (L, g, ms)
+        del tree
+    ch = Choice(levels=best[0], threads_per_query=best[1], ms=best[2], plain_levels=L0, table=table)
+    if use_cache:
+        cache[key] = asdict(ch)
+        _store_cache(cache)
+    return ch
+
+
+def build_tuned_kd_tree(points_ref: torch.Tensor, queries: torch.Tensor, k: int, **kw) -> TorchKDTree:
+    """build_kd_tree with the autotuned depth and lanes per query."""
+    ch = autotune(points_ref, queries, k, **kw)
+    return build_kd_tree(points_ref, levels=ch.levels, query_opts=QueryOpts.make(threads_per_query=ch.threads_per_query))

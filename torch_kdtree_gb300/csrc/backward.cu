@@ -1,0 +1,198 @@
+// Deterministic backward of the KNN squared distances.
+//
+// Forward: dist[i, j] = sum_c (q[i, c] - ref[m, c])^2 with m = idx[i, j].
+// The reference differentiates a torch re-gather of these distances
+// (torch_kdtree/nn_distance.py:111-112), whose ref gradient goes through
+// index_put_ with accumulate -- float atomics, run-to-run nondeterministic.
+// Here:
+//   grad_q[i]   = sum_j 2 g[i, j] (q[i] - ref[idx[i, j]])       (a gather, j ascending)
+//   grad_ref[m] = sum_{(i,j): idx[i,j] = m} 2 g[i, j] (ref[m] - q[i])
+// grad_ref is a segmented reduction: the (idx, pair) list is sorted by a
+// stable radix sort, so each reference point sees its pairs in ascending
+// pair order and one thread sums them in that fixed order -- bitwise
+// reproducible, no float atomics.  Differences are recomputed from the saved
+// indices; nothing of size [Q, k, d] is stored.
+#include <algorithm>
+#include <string>
+
+#include "sort.cuh"
+#include "tk_internal.h"
+
+namespace tk {
+namespace {
+
+size_t align256(size_t v) { return (v + 255) / 256 * 256; }
+
+template <typename T, int D>
+__global__ void k_grad_q(const T* __restrict__ q, const T* __restrict__ ref, const int32_t* __restrict__ idx,
+                         const T* __restrict__ g, int nq, int n, int k, T* __restrict__ grad_q) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nq) return;
+    T qi[D], acc[D];
+#pragma unroll
+    for (int c = 0; c < D; ++c) {
+        qi[c] = q[(long long)i * D + c];
+        acc[c] = T(0);
+    }
+    for (int j = 0; j < k; ++j) {
+        const int m = idx[(long long)i * k + j];
+        if (m < 0 || m >= n) continue;
+        const T w = T(2) * g[(long long)i * k + j];
+#pragma unroll
+        for (int c = 0; c < D; ++c) acc[c] += w * (qi[c] - ref[(long long)m * D + c]);
+    }
+#pragma unroll
+    for (int c = 0; c < D; ++c) grad_q[(long long)i * D + c] = acc[c];
+}
+
+// keys: neighbour index (n for invalid entries, which sort last).
+__global__ void k_make_keys(const int32_t* __restrict__ idx, long long npairs, int n, uint32_t* __restrict__ keys) {
+    const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= npairs) return;
+    const int m = idx[p];
+    keys[p] = (m < 0 || m >= n) ? uint32_t(n) : uint32_t(m);
+}
+
+// Segment bounds of every key present in the sorted list: seg_start[m] and
+// seg_end[m] (one past the last position).  Keys absent from the list keep
+// seg_end[m] = 0 (zeroed beforehand) and are skipped.
+__global__ void k_segment_bounds(const uint32_t* __restrict__ keys, long long npairs, int n,
+                                 int* __restrict__ seg_start, int* __restrict__ seg_end) {
+    const long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= npairs) return;
+    const uint32_t key = keys[s];
+    if (key >= uint32_t(n)) return;
+    if (s == 0 || keys[s - 1] != key) seg_start[key] = int(s);
+    if (s == npairs - 1 || keys[s + 1] != key) seg_end[key] = int(s + 1);
+}
+
+// One thread per reference point walks its segment in sorted (ascending
+// pair) order.
+template <typename T, int D>
+__global__ void k_grad_ref(const T* __restrict__ q, const T* __restrict__ ref, const T* __restrict__ g,
+                           const uint32_t* __restrict__ pairs, const int* __restrict__ seg_start,
+                           const int* __restrict__ seg_end, int n, int k, T* __restrict__ grad_ref) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= n) return;
+    T rm[D], acc[D];
+#pragma unroll
+    for (int c = 0; c < D; ++c) {
+        rm[c] = ref[(long long)m * D + c];
+        acc[c] = T(0);
+    }
+    const int end = seg_end[m];
+    const int beg = end > 0 ? seg_start[m] : 0;  // seg_start is only written for keys present
+    for (int s = beg; s < end; ++s) {
+        const uint32_t p = pairs[s];
+        const long long i = (long long)(p / uint32_t(k));
+        const T w = T(2) * g[p];
+#pragma unroll
+        for (int c = 0; c < D; ++c) acc[c] += w * (rm[c] - q[i * D + c]);
+    }
+#pragma unroll
+    for (int c = 0; c < D; ++c) grad_ref[(long long)m * D + c] = acc[c];
+}
+
+struct BwLayout {
+    size_t keys = 0, sorted_keys = 0, sorted_vals = 0, seg_end = 0, seg_start = 0, sort_ws = 0, total = 0;
+};
+
+BwLayout bw_layout(int64_t nq, int k, int64_t n) {
+    BwLayout w;
+    const int64_t np = std::max<int64_t>(1, nq * k);
+    size_t o = 0;
+    w.keys = o;
+    o += align256(4 * size_t(np));
+    w.sorted_keys = o;
+    o += align256(4 * size_t(np));
+    w.sorted_vals = o;
+    o += align256(4 * size_t(np));
+    w.seg_end = o;
+    o += align256(4 * size_t(std::max<int64_t>(n, 1)));
+    w.seg_start = o;
+    o += align256(4 * size_t(std::max<int64_t>(n, 1)));
+    w.sort_ws = o;
+    o += sort_workspace_bytes(np);
+    w.total = o;
+    return w;
+}
+
+int key_bits_for(int64_t n) {
+    int b = 1;
+    while ((int64_t(1) << b) <= n) ++b;  // keys 0..n inclusive (n marks invalid)
+    return b;
+}
+
+template <typename T, int D>
+int run_backward(const T* q, const T* ref, const int32_t* idx, const T* g, int nq, int n, int k, T* grad_q,
+                 T* grad_ref, char* ws, cudaStream_t s) {
+    if (grad_q) k_grad_q<T, D><<<(nq + 255) / 256, 256, 0, s>>>(q, ref, idx, g, nq, n, k, grad_q);
+    if (grad_ref) {
+        const BwLayout w = bw_layout(nq, k, n);
+        const long long np = (long long)nq * k;
+        uint32_t* keys = reinterpret_cast<uint32_t*>(ws + w.keys);
+        uint32_t* sk = reinterpret_cast<uint32_t*>(ws + w.sorted_keys);
+        uint32_t* sv = reinterpret_cast<uint32_t*>(ws + w.sorted_vals);
+        int* seg_end = reinterpret_cast<int*>(ws + w.seg_end);
+        int* seg_start = reinterpret_cast<int*>(ws + w.seg_start);
+        if (np > 0) {
+            k_make_keys<<<unsigned((np + 255) / 256), 256, 0, s>>>(idx, np, n, keys);
+            cudaError_t e = sort_pairs(keys, nullptr, sk, sv, np, key_bits_for(n), ws + w.sort_ws,
+                                       sort_workspace_bytes(np), s);
+            if (e != cudaSuccess) return fail(TK_ECUDA, std::string("backward sort: ") + cudaGetErrorString(e));
+        }
+        cudaError_t e = cudaMemsetAsync(seg_end, 0, sizeof(int) * size_t(n), s);
+        if (e != cudaSuccess) return fail(TK_ECUDA, std::string("memset: ") + cudaGetErrorString(e));
+        if (np > 0) k_segment_bounds<<<unsigned((np + 255) / 256), 256, 0, s>>>(sk, np, n, seg_start, seg_end);
+        k_grad_ref<T, D><<<(n + 255) / 256, 256, 0, s>>>(q, ref, g, sv, seg_start, seg_end, n, k, grad_ref);
+    }
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(TK_ECUDA, std::string("backward launch: ") + cudaGetErrorString(e));
+    return TK_OK;
+}
+
+}  // namespace
+}  // namespace tk
+
+using namespace tk;
+
+extern "C" {
+
+size_t tk_knn_backward_workspace_size(int64_t nq, int k, int64_t n) {
+    if (nq < 0 || k < 1 || n < 1) return 0;
+    return bw_layout(nq, k, n).total;
+}
+
+int tk_knn_backward(const void* q, const void* ref, const int32_t* idx, const void* grad_dists, int64_t nq,
+                    int64_t n, int k, int dims, int dtype, void* grad_q, void* grad_ref, void* workspace,
+                    size_t workspace_bytes, void* stream) {
+    clear_error();
+    if (nq < 0 || nq >= (int64_t(1) << 31) || n < 1 || n >= (int64_t(1) << 31) || k < 1)
+        return fail(TK_EINVAL, "bad sizes");
+    if (nq * int64_t(k) >= (int64_t(1) << 31)) return fail(TK_EINVAL, "nq * k must be < 2^31");
+    if (dims < 1 || dims > 3) return fail(TK_EINVAL, "dims must be 1, 2 or 3");
+    if (dtype != TK_F32 && dtype != TK_F64) return fail(TK_EINVAL, "dtype must be TK_F32 or TK_F64");
+    if (nq == 0 && !grad_ref) return TK_OK;
+    if (!q || !ref || !idx || !grad_dists) return fail(TK_EINVAL, "null input pointer");
+    if (grad_ref && (!workspace || workspace_bytes < bw_layout(nq, k, n).total))
+        return fail(TK_EWORKSPACE, "workspace too small");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    char* ws = static_cast<char*>(workspace);
+    const int nq32 = int(nq), n32 = int(n);
+#define TK_BW(TT, DD)                                                                                       \
+    return run_backward<TT, DD>(static_cast<const TT*>(q), static_cast<const TT*>(ref), idx,                \
+                                static_cast<const TT*>(grad_dists), nq32, n32, k, static_cast<TT*>(grad_q), \
+                                static_cast<TT*>(grad_ref), ws, s)
+    if (dtype == TK_F32) {
+        if (dims == 1) TK_BW(float, 1);
+        if (dims == 2) TK_BW(float, 2);
+        TK_BW(float, 3);
+    } else {
+        if (dims == 1) TK_BW(double, 1);
+        if (dims == 2) TK_BW(double, 2);
+        TK_BW(double, 3);
+    }
+#undef TK_BW
+}
+
+}  // extern "C"

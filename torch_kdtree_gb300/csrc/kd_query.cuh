@@ -1,0 +1,217 @@
+// Exact KD-tree KNN query kernels (sm_103a).
+//
+// What the reference does (src/kdtree_g.cu:286-457): one query per 64-thread
+// block, thread 0 alone walks the tree with 2-bit visited tags in shared
+// memory, leaf distances go through a 256-entry shared buffer and every
+// candidate is inserted serially with a block barrier.
+//
+// What this file does instead:
+//  1. Queries are first binned by the tree cell they fall into (a counting
+//     sort over the cells at depth B), so neighbouring lanes follow nearly
+//     the same path through the tree and hit the same leaves in L1.
+//  2. A group of G lanes (G = 1..32, "threads per query") serves one query.
+//     The walk is a depth-first descent with an explicit short stack of far
+//     siblings; each entry carries the per-axis squared plane distances of
+//     its cell, whose rounded sum is a lower bound on every distance inside
+//     (exactly safe under round-to-nearest, see sqdist), so pruning never
+//     drops a neighbour and the result equals an exhaustive search ordered by
+//     (distance, original index) -- independent of tree shape and launch
+//     shape.
+//  3. The top split levels are staged in shared memory; deeper split values
+//     and the leaf buckets (16-byte point records: xyz + original index) are
+//     read through the read-only path, coalesced across the G lanes.
+//  4. The k best keys live in registers, distributed over the group
+//     (TopK in tk_device.cuh); candidates are offered in lane order.
+//  5. Warps pull work from a global counter (persistent grid sized to the
+//     SM count), so no block waits for a slow neighbour.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "tk_device.cuh"
+#include "tk_internal.h"
+
+namespace tk {
+
+template <typename T>
+struct KdArgs {
+    const PointRec<T>* pts;  // [n] in leaf order
+    const T* medians;        // [2^L - 1] heap order
+    const int32_t* leaf_off; // [2^L + 1]
+    int levels;              // L
+    int smem_levels;         // S <= L: levels staged in shared memory
+    const T* q;              // [nq, D]
+    int nq;
+    int k;
+    const int32_t* order;    // [nq] processing order (binned), or null for identity
+    T* out_d;                // [nq, k]
+    int32_t* out_i;          // [nq, k]
+    int* work;               // global work counter, zero at launch
+};
+
+template <typename T, int D>
+struct StackEntry {
+    int node;
+    T e[D];  // per-axis squared distance from the query to the cell's slab
+};
+
+template <typename T, int D>
+__device__ __forceinline__ T cell_bound(const T (&e)[D]) {
+    T b = e[0];
+    if (D > 1) b = add_rn(b, e[1]);
+    if (D > 2) b = add_rn(b, e[2]);
+    return b;
+}
+
+template <typename T, int D>
+__device__ __forceinline__ T pick(const T (&v)[D], int ax) {
+    T r = v[0];
+    if (D > 1) r = ax == 1 ? v[1] : r;
+    if (D > 2) r = ax == 2 ? v[2] : r;
+    return r;
+}
+
+// Exhaustive-equivalent KNN for one query, served by a group of G lanes.
+template <typename T, int D, int G, int R>
+__device__ __forceinline__ void kd_query_one(const KdArgs<T>& a, const T* s_med, int qi, unsigned gmask,
+                                             int gl, int gbase) {
+    T q[D];
+#pragma unroll
+    for (int c = 0; c < D; ++c) q[c] = a.q[(long long)qi * D + c];
+
+    TopK<T, G, R> list;
+    list.init(a.k, gl);
+    Key<T> worst = Key<T>::sentinel();
+    T worst_d = worst.dist();
+
+    StackEntry<T, D> stk[kMaxLevels];
+    int sp = 0;
+    int node = 0, depth = 0;
+    T e[D];
+#pragma unroll
+    for (int c = 0; c < D; ++c) e[c] = T(0);
+    const int L = a.levels;
+    const int first_leaf = (1 << L) - 1;
+
+    for (;;) {
+        // descend to the near leaf, stacking far siblings that may matter
+        int ax = depth % D;
+        while (depth < L) {
+            const T m = depth < a.smem_levels ? s_med[node] : __ldg(a.medians + node);
+            const T qa = pick<T, D>(q, ax);
+            const T diff = sub_rn(qa, m);
+            const T plane = mul_rn(diff, diff);
+            const bool go_left = qa < m;  // src/kdtree.cpp:30
+            StackEntry<T, D> far;
+            far.node = 2 * node + (go_left ? 2 : 1);
+#pragma unroll
+            for (int c = 0; c < D; ++c) far.e[c] = (c == ax) ? plane : e[c];
+            if (cell_bound<T, D>(far.e) <= worst_d) stk[sp++] = far;
+            node = 2 * node + (go_left ? 1 : 2);
+            ++depth;
+            ax = (ax + 1 == D) ? 0 : ax + 1;
+        }
+        // scan the leaf bucket, G points at a time
+        {
+            const int leaf = node - first_leaf;
+            const int beg = __ldg(a.leaf_off + leaf);
+            const int end = __ldg(a.leaf_off + leaf + 1);
+            for (int j0 = beg; j0 < end; j0 += G) {
+                const int j = j0 + gl;
+                Key<T> mine = Key<T>::sentinel();
+                if (j < end) {
+                    const PointRec<T> p = load_rec(a.pts + j);
+                    mine = Key<T>::make(sqdist<T, D>(q, p), rec_index(p));
+                }
+                worst = offer<T, G, R>(list, mine, worst, gmask, gl, gbase);
+            }
+            worst_d = worst.dist();
+        }
+        // resume at the deepest stacked cell that can still hold a neighbour
+        bool resumed = false;
+        while (sp > 0) {
+            const StackEntry<T, D> s = stk[--sp];
+            if (cell_bound<T, D>(s.e) <= worst_d) {
+                node = s.node;
+#pragma unroll
+                for (int c = 0; c < D; ++c) e[c] = s.e[c];
+                depth = 31 - __clz(node + 1);
+                resumed = true;
+                break;
+            }
+        }
+        if (!resumed) break;
+    }
+    list.store(a.k, gl, a.out_d, a.out_i, qi);
+}
+
+template <typename T, int D, int G, int R>
+__global__ void __launch_bounds__(256) k_kd_query(const KdArgs<T> a) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* s_med = reinterpret_cast<T*>(smem_raw);
+    const int n_smem = (1 << a.smem_levels) - 1;
+    for (int i = threadIdx.x; i < n_smem; i += blockDim.x) s_med[i] = a.medians[i];
+    __syncthreads();
+
+    const int lane = threadIdx.x & 31;
+    const int gl = lane & (G - 1);
+    const int gbase = lane & ~(G - 1);
+    const unsigned gmask = group_mask<G>(lane);
+    constexpr int kGroupsPerWarp = 32 / G;
+    const int gid = lane / G;
+
+    for (;;) {
+        int base = 0;
+        if (lane == 0) base = atomicAdd(a.work, kGroupsPerWarp);
+        base = __shfl_sync(0xFFFFFFFFu, base, 0);
+        if (base >= a.nq) break;
+        const int t = base + gid;
+        if (t < a.nq) {
+            const int qi = a.order ? __ldg(a.order + t) : t;
+            kd_query_one<T, D, G, R>(a, s_med, qi, gmask, gl, gbase);
+        }
+        __syncwarp();
+    }
+}
+
+// ---------------------------------------------------------- query binning --
+
+// Cell id at depth B of every query (same descent rule as the search) and
+// its arrival rank within the cell.
+template <typename T, int D>
+__global__ void k_bin_count(const T* __restrict__ q, int nq, const T* __restrict__ medians, int B,
+                            int* __restrict__ counts, int* __restrict__ bin_of, int* __restrict__ pos_of) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nq) return;
+    T p[D];
+#pragma unroll
+    for (int c = 0; c < D; ++c) p[c] = q[(long long)i * D + c];
+    int node = 0, ax = 0;
+    for (int depth = 0; depth < B; ++depth) {
+        const T m = __ldg(medians + node);
+        node = 2 * node + (pick<T, D>(p, ax) < m ? 1 : 2);
+        ax = (ax + 1 == D) ? 0 : ax + 1;
+    }
+    const int bin = node - ((1 << B) - 1);
+    bin_of[i] = bin;
+    pos_of[i] = atomicAdd(counts + bin, 1);
+}
+
+__global__ void k_bin_scan(int* counts, int nbins, int* work);
+__global__ void k_bin_scatter(int nq, const int* bin_of, const int* pos_of, const int* offsets, int* order);
+
+// Per-(T, D) launcher implemented in kd_query_<type>_d<D>.cu.
+struct KdLaunch {
+    int G, R;
+    int block, grid;
+    size_t smem;
+};
+template <typename T, int D>
+int kd_query_launch(const KdArgs<T>& a, const KdLaunch& l, cudaStream_t s);
+template <typename T, int D>
+const void* kd_query_kernel(int G, int R);
+template <typename T, int D>
+void bin_count_launch(const T* q, int nq, const T* medians, int B, int* counts, int* bin_of, int* pos_of,
+                      cudaStream_t s);
+
+}  // namespace tk

@@ -1,0 +1,438 @@
+// C ABI of the engine (include/tk_knn.h): error reporting, tree life cycle,
+// and the KD query pipeline (query binning + KD kernel launch).
+#include <algorithm>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "kd_query.cuh"
+#include "tk_internal.h"
+
+namespace tk {
+
+namespace {
+thread_local std::string g_err;
+
+struct DeviceGuard {
+    int prev = -1;
+    bool changed = false;
+    explicit DeviceGuard(int dev) {
+        if (cudaGetDevice(&prev) == cudaSuccess && prev != dev) {
+            changed = cudaSetDevice(dev) == cudaSuccess;
+        }
+    }
+    ~DeviceGuard() {
+        if (changed) cudaSetDevice(prev);
+    }
+};
+
+int sm_count(int dev) {
+    static std::mutex mu;
+    static std::vector<int> cache;
+    std::lock_guard<std::mutex> lock(mu);
+    if (dev < 0) dev = 0;
+    if ((int)cache.size() <= dev) cache.resize(dev + 1, 0);
+    if (cache[dev] == 0) {
+        int v = 0;
+        if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0) v = 1;
+        cache[dev] = v;
+    }
+    return cache[dev];
+}
+
+size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+}  // namespace
+
+int fail(int status, const std::string& msg) {
+    g_err = msg;
+    return status;
+}
+void clear_error() { g_err.clear(); }
+
+// ------------------------------------------------------------ binning --
+
+__global__ void k_bin_scan(int* counts, int nbins, int* work) {
+    // One block of 1024 threads: exclusive scan of counts[0..nbins) in place.
+    __shared__ int warp_sums[32];
+    const int tid = threadIdx.x;
+    const int per = (nbins + blockDim.x - 1) / blockDim.x;
+    const int beg = min(nbins, tid * per), end = min(nbins, beg + per);
+    int sum = 0;
+    for (int i = beg; i < end; ++i) sum += counts[i];
+    // inclusive scan of per-thread sums
+    const int lane = tid & 31, wid = tid >> 5;
+    int v = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(0xFFFFFFFFu, v, o);
+        if (lane >= o) v += t;
+    }
+    if (lane == 31) warp_sums[wid] = v;
+    __syncthreads();
+    if (wid == 0) {
+        int w = lane < (int)(blockDim.x >> 5) ? warp_sums[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(0xFFFFFFFFu, w, o);
+            if (lane >= o) w += t;
+        }
+        warp_sums[lane] = w;
+    }
+    __syncthreads();
+    int run = v - sum + (wid > 0 ? warp_sums[wid - 1] : 0);
+    for (int i = beg; i < end; ++i) {
+        const int c = counts[i];
+        counts[i] = run;
+        run += c;
+    }
+    if (tid == 0) *work = 0;
+}
+
+__global__ void k_bin_scatter(int nq, const int* bin_of, const int* pos_of, const int* offsets, int* order) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nq) return;
+    order[offsets[bin_of[i]] + pos_of[i]] = i;
+}
+
+// ------------------------------------------------------------ planning --
+
+namespace {
+
+int bin_levels(int L, int64_t nq) {
+    int lg = 0;
+    while ((int64_t(1) << (lg + 1)) <= nq) ++lg;
+    return std::max(1, std::min({L, kMaxBinLevels, lg - 4}));
+}
+
+struct WsLayout {
+    size_t counter = 0, counts = 0, bin_of = 0, pos_of = 0, order = 0, total = 0;
+};
+
+WsLayout ws_layout(int L, int64_t nq) {
+    WsLayout w;
+    const int B = bin_levels(L, nq);
+    size_t o = 0;
+    w.counter = o;
+    o += 256;
+    w.counts = o;
+    o += align_up(sizeof(int) * (size_t(1) << B), 256);
+    w.bin_of = o;
+    o += align_up(sizeof(int) * size_t(nq), 256);
+    w.pos_of = o;
+    o += align_up(sizeof(int) * size_t(nq), 256);
+    w.order = o;
+    o += align_up(sizeof(int) * size_t(nq), 256);
+    w.total = o;
+    return w;
+}
+
+bool gr_available(int dtype, int dims, int G, int R) {
+    const bool full = dtype == TK_F32 && dims == 3;
+    if (!full && !(G == 1 || G == 4 || G == 32)) return false;
+    if (R < 1 || R > 16 || (R & (R - 1))) return false;
+    if (G * R > 128) return false;
+    if (G == 16 && R > 8) return false;
+    if (G == 32 && R > 4) return false;
+    return true;
+}
+
+int auto_lanes(const tk_tree* t) {
+    const double avg_leaf = double(t->n) / double(int64_t(1) << t->levels);
+    if (avg_leaf <= 24) return 1;
+    if (avg_leaf <= 48) return 2;
+    if (avg_leaf <= 96) return 4;
+    if (avg_leaf <= 192) return 8;
+    if (avg_leaf <= 384) return 16;
+    return 32;
+}
+
+int pow2_ceil(int v) {
+    int p = 1;
+    while (p < v) p <<= 1;
+    return p;
+}
+
+template <typename T, int D>
+int run_query(const tk_tree* t, const T* q, int nq, int k, T* dists, int32_t* idx, const tk_query_opts& o,
+              char* ws, cudaStream_t s) {
+    // lanes per query and registers per lane
+    int G = o.threads_per_query > 0 ? o.threads_per_query : auto_lanes(t);
+    if (G != 1 && G != 2 && G != 4 && G != 8 && G != 16 && G != 32)
+        return fail(TK_EINVAL, "threads_per_query must be 1, 2, 4, 8, 16 or 32");
+    G = std::max(G, pow2_ceil((k + 15) / 16));
+    int R = pow2_ceil((k + G - 1) / G);
+    while (!gr_available(t->dtype, D, G, R) && G < 32) {
+        G <<= 1;
+        R = pow2_ceil((k + G - 1) / G);
+    }
+    if (!gr_available(t->dtype, D, G, R)) return fail(TK_EUNSUPPORTED, "no kernel shape for this k");
+
+    const int L = t->levels;
+    int S = o.smem_levels >= 0 ? o.smem_levels : (sizeof(T) == 4 ? 12 : 11);
+    S = std::max(0, std::min({S, L, sizeof(T) == 4 ? 15 : 14}));  // <= 128 KiB of shared memory
+    const int block = 256;
+    const size_t smem = sizeof(T) * ((size_t(1) << S) - 1);
+    const void* kfn = kd_query_kernel<T, D>(G, R);
+    if (!kfn) return fail(TK_EUNSUPPORTED, "KD query kernel shape not compiled");
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+        if (e != cudaSuccess) return fail(TK_ECUDA, std::string("smem attribute: ") + cudaGetErrorString(e));
+    }
+    int per_sm = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, block, smem);
+    if (e != cudaSuccess || per_sm <= 0) per_sm = 1;
+    if (o.blocks_per_sm > 0) per_sm = std::min(per_sm, int(o.blocks_per_sm));
+    const int groups_per_block = block / G;
+    const int need = (nq + groups_per_block - 1) / groups_per_block;
+    const int grid = std::max(1, std::min(need, per_sm * sm_count(t->device)));
+
+    const WsLayout w = ws_layout(L, nq);
+    int* counter = reinterpret_cast<int*>(ws + w.counter);
+    const bool bin = o.bin_queries == 1 || (o.bin_queries < 0 && nq >= 1024 && L >= 2);
+    const int32_t* order = nullptr;
+    if (bin) {
+        const int B = bin_levels(L, nq);
+        const int nbins = 1 << B;
+        int* counts = reinterpret_cast<int*>(ws + w.counts);
+        int* bin_of = reinterpret_cast<int*>(ws + w.bin_of);
+        int* pos_of = reinterpret_cast<int*>(ws + w.pos_of);
+        int* ord = reinterpret_cast<int*>(ws + w.order);
+        e = cudaMemsetAsync(counts, 0, sizeof(int) * nbins, s);
+        if (e != cudaSuccess) return fail(TK_ECUDA, std::string("memset: ") + cudaGetErrorString(e));
+        bin_count_launch<T, D>(q, nq, static_cast<const T*>(t->d_medians), B, counts, bin_of, pos_of, s);
+        k_bin_scan<<<1, 1024, 0, s>>>(counts, nbins, counter);
+        k_bin_scatter<<<(nq + 255) / 256, 256, 0, s>>>(nq, bin_of, pos_of, counts, ord);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return fail(TK_ECUDA, std::string("binning launch: ") + cudaGetErrorString(e));
+        order = ord;
+    } else {
+        e = cudaMemsetAsync(counter, 0, sizeof(int), s);
+        if (e != cudaSuccess) return fail(TK_ECUDA, std::string("memset: ") + cudaGetErrorString(e));
+    }
+
+    KdArgs<T> a;
+    a.pts = static_cast<const PointRec<T>*>(t->d_pts);
+    a.medians = static_cast<const T*>(t->d_medians);
+    a.leaf_off = t->d_leaf_off;
+    a.levels = L;
+    a.smem_levels = S;
+    a.q = q;
+    a.nq = nq;
+    a.k = k;
+    a.order = order;
+    a.out_d = dists;
+    a.out_i = idx;
+    a.work = counter;
+    KdLaunch l{G, R, block, grid, smem};
+    if (o.kernel_start_event) cudaEventRecord(static_cast<cudaEvent_t>(o.kernel_start_event), s);
+    const int rc = kd_query_launch<T, D>(a, l, s);
+    if (rc == TK_OK && o.kernel_stop_event) cudaEventRecord(static_cast<cudaEvent_t>(o.kernel_stop_event), s);
+    return rc;
+}
+
+template <typename T>
+int upload_tree(tk_tree* t, const HostTree<T>& h) {
+    const int64_t n = h.n;
+    std::vector<PointRec<T>> recs(static_cast<size_t>(n));
+    for (int64_t i = 0; i < n; ++i) {
+        T c[3] = {T(0), T(0), T(0)};
+        for (int d = 0; d < h.dims; ++d) c[d] = h.structured[i * h.dims + d];
+        recs[i].x = c[0];
+        recs[i].y = c[1];
+        recs[i].z = c[2];
+        if (sizeof(T) == 4) {
+            uint32_t bits = uint32_t(h.perm[i]);
+            std::memcpy(&recs[i].w, &bits, 4);
+        } else {
+            uint64_t bits = uint64_t(uint32_t(h.perm[i]));
+            std::memcpy(&recs[i].w, &bits, 8);
+        }
+    }
+    const size_t b_pts = sizeof(PointRec<T>) * size_t(n);
+    const size_t b_med = sizeof(T) * h.medians.size();
+    const size_t b_off = sizeof(int32_t) * h.leaf_off.size();
+    cudaError_t e = cudaMalloc(&t->d_pts, b_pts);
+    if (e == cudaSuccess) e = cudaMalloc(&t->d_medians, std::max<size_t>(b_med, sizeof(T)));
+    if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&t->d_leaf_off), b_off);
+    if (e != cudaSuccess) return fail(TK_ENOMEM, std::string("device allocation: ") + cudaGetErrorString(e));
+    e = cudaMemcpy(t->d_pts, recs.data(), b_pts, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && b_med) e = cudaMemcpy(t->d_medians, h.medians.data(), b_med, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(t->d_leaf_off, h.leaf_off.data(), b_off, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return fail(TK_ECUDA, std::string("tree upload: ") + cudaGetErrorString(e));
+    t->device_bytes = int64_t(b_pts + b_med + b_off);
+    return TK_OK;
+}
+
+void free_tree_device(tk_tree* t) {
+    if (t->d_pts) cudaFree(t->d_pts);
+    if (t->d_medians) cudaFree(t->d_medians);
+    if (t->d_leaf_off) cudaFree(t->d_leaf_off);
+    t->d_pts = t->d_medians = nullptr;
+    t->d_leaf_off = nullptr;
+}
+
+}  // namespace
+}  // namespace tk
+
+using namespace tk;
+
+extern "C" {
+
+const char* tk_last_error(void) { return g_err.c_str(); }
+
+int tk_version(void) { return 1; }
+
+int tk_cuda_available(void) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n > 0 ? 1 : 0;
+}
+
+int tk_tree_create(const void* host_points, int64_t n, int dims, int dtype, int levels, int device,
+                   int n_threads, tk_tree** out) {
+    clear_error();
+    if (!out) return fail(TK_EINVAL, "out is null");
+    *out = nullptr;
+    if (dtype != TK_F32 && dtype != TK_F64) return fail(TK_EINVAL, "dtype must be TK_F32 or TK_F64");
+    tk_tree* t = new (std::nothrow) tk_tree();
+    if (!t) return fail(TK_ENOMEM, "host allocation failed");
+    t->dtype = dtype;
+    t->dims = dims;
+    t->levels = levels;
+    t->device = device;
+    t->n = n;
+    int rc = dtype == TK_F32
+                 ? build_host_tree<float>(static_cast<const float*>(host_points), n, dims, levels, n_threads, t->h32)
+                 : build_host_tree<double>(static_cast<const double*>(host_points), n, dims, levels, n_threads,
+                                           t->h64);
+    if (rc != TK_OK) {
+        delete t;
+        return rc;
+    }
+    if (device < 0) {  // host-only tree: layout getters work, queries are refused
+        *out = t;
+        return TK_OK;
+    }
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || device >= ndev) {
+        cudaGetLastError();
+        delete t;
+        return fail(TK_EINVAL, "CUDA device " + std::to_string(device) + " is not available");
+    }
+    {
+        DeviceGuard g(device);
+        rc = dtype == TK_F32 ? upload_tree<float>(t, t->h32) : upload_tree<double>(t, t->h64);
+    }
+    if (rc != TK_OK) {
+        DeviceGuard g(device);
+        free_tree_device(t);
+        delete t;
+        return rc;
+    }
+    *out = t;
+    return TK_OK;
+}
+
+int tk_tree_destroy(tk_tree* t) {
+    clear_error();
+    if (!t) return TK_OK;
+    if (t->device >= 0) {
+        DeviceGuard g(t->device);
+        free_tree_device(t);
+    }
+    delete t;
+    return TK_OK;
+}
+
+int tk_tree_get_info(const tk_tree* t, tk_tree_info* out) {
+    if (!t || !out) return fail(TK_EINVAL, "null argument");
+    out->n_points = t->n;
+    out->dims = t->dims;
+    out->dtype = t->dtype;
+    out->levels = t->levels;
+    out->device = t->device;
+    out->n_leaves = int64_t(1) << t->levels;
+    out->device_bytes = t->device_bytes;
+    return TK_OK;
+}
+
+int tk_tree_get_perm(const tk_tree* t, int32_t* out) {
+    if (!t || !out) return fail(TK_EINVAL, "null argument");
+    const auto& p = t->dtype == TK_F32 ? t->h32.perm : t->h64.perm;
+    std::memcpy(out, p.data(), sizeof(int32_t) * p.size());
+    return TK_OK;
+}
+
+int tk_tree_get_points(const tk_tree* t, void* out) {
+    if (!t || !out) return fail(TK_EINVAL, "null argument");
+    if (t->dtype == TK_F32)
+        std::memcpy(out, t->h32.structured.data(), sizeof(float) * t->h32.structured.size());
+    else
+        std::memcpy(out, t->h64.structured.data(), sizeof(double) * t->h64.structured.size());
+    return TK_OK;
+}
+
+int tk_tree_get_splits(const tk_tree* t, void* medians, int32_t* leaf_offsets) {
+    if (!t) return fail(TK_EINVAL, "null argument");
+    if (medians) {
+        if (t->dtype == TK_F32)
+            std::memcpy(medians, t->h32.medians.data(), sizeof(float) * t->h32.medians.size());
+        else
+            std::memcpy(medians, t->h64.medians.data(), sizeof(double) * t->h64.medians.size());
+    }
+    if (leaf_offsets) {
+        const auto& o = t->dtype == TK_F32 ? t->h32.leaf_off : t->h64.leaf_off;
+        std::memcpy(leaf_offsets, o.data(), sizeof(int32_t) * o.size());
+    }
+    return TK_OK;
+}
+
+size_t tk_tree_query_workspace_size(const tk_tree* t, int64_t nq) {
+    if (!t || nq < 0) return 0;
+    return ws_layout(t->levels, std::max<int64_t>(nq, 1)).total;
+}
+
+int tk_tree_query(const tk_tree* t, const void* q, int64_t nq, int k, void* dists, int32_t* idx,
+                  const tk_query_opts* opts, void* workspace, size_t workspace_bytes, void* stream) {
+    clear_error();
+    if (!t) return fail(TK_EINVAL, "tree is null");
+    if (nq < 0 || nq >= (int64_t(1) << 31)) return fail(TK_EINVAL, "number of queries must be in [0, 2^31)");
+    if (k < 1) return fail(TK_EINVAL, "k must be >= 1");
+    if (k > t->n) return fail(TK_EINVAL, "You requested more nearest neighbors than there are in the KD-Tree");
+    if (k > kMaxK) return fail(TK_EINVAL, "k is limited to 128 on the GPU");
+    if (t->device < 0 || !t->d_pts) return fail(TK_EINVAL, "tree was built host-only (device < 0); it has no device image");
+    if (nq == 0) return TK_OK;
+    if (!q || !dists || !idx) return fail(TK_EINVAL, "null query or output pointer");
+    const size_t need = ws_layout(t->levels, nq).total;
+    if (!workspace || workspace_bytes < need)
+        return fail(TK_EWORKSPACE, "workspace too small: need " + std::to_string(need) + " bytes");
+    tk_query_opts o{0, -1, -1, 0, 0, nullptr, nullptr};
+    if (opts) o = *opts;
+    DeviceGuard g(t->device);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    char* ws = static_cast<char*>(workspace);
+    const int n32 = int(nq);
+    if (t->dtype == TK_F32) {
+        auto* qq = static_cast<const float*>(q);
+        auto* dd = static_cast<float*>(dists);
+        switch (t->dims) {
+            case 1: return run_query<float, 1>(t, qq, n32, k, dd, idx, o, ws, s);
+            case 2: return run_query<float, 2>(t, qq, n32, k, dd, idx, o, ws, s);
+            default: return run_query<float, 3>(t, qq, n32, k, dd, idx, o, ws, s);
+        }
+    } else {
+        auto* qq = static_cast<const double*>(q);
+        auto* dd = static_cast<double*>(dists);
+        switch (t->dims) {
+            case 1: return run_query<double, 1>(t, qq, n32, k, dd, idx, o, ws, s);
+            case 2: return run_query<double, 2>(t, qq, n32, k, dd, idx, o, ws, s);
+            default: return run_query<double, 3>(t, qq, n32, k, dd, idx, o, ws, s);
+        }
+    }
+}
+
+}  // extern "C"

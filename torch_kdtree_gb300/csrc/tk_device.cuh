@@ -1,0 +1,217 @@
+// Device-side building blocks shared by the KNN kernels.
+//
+//  * PointRec<T>: a reference point as stored in HBM -- three coordinates
+//    (zero-padded below three dimensions) and the ORIGINAL index in the
+//    fourth slot, so one 16-byte (f32) load yields everything a candidate
+//    needs and the remap through shuffled_inds (torch_kdtree/nn_distance.py:109)
+//    disappears.
+//  * Key<T>: (squared distance, original index) packed so that an unsigned
+//    compare orders candidates by distance, then by lower index.
+//  * sqdist<T, D>: the reference's distance arithmetic, bit for bit:
+//    d_c = q_c - r_c, s = ((0 + d0*d0) + d1*d1) + d2*d2, every operation
+//    rounded separately (src/kdtree.hpp:546-591).  The _rn intrinsics keep
+//    the compiler from fusing multiply and add.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace tk {
+
+template <typename T>
+struct alignas(4 * sizeof(T)) PointRec {
+    T x, y, z, w;  // w holds the original index as raw bits
+};
+
+__device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+
+__device__ __forceinline__ PointRec<float> load_rec(const PointRec<float>* p) {
+    const float4 v = __ldg(reinterpret_cast<const float4*>(p));
+    return PointRec<float>{v.x, v.y, v.z, v.w};
+}
+__device__ __forceinline__ PointRec<double> load_rec(const PointRec<double>* p) {
+    const double2 a = __ldg(reinterpret_cast<const double2*>(p));
+    const double2 b = __ldg(reinterpret_cast<const double2*>(p) + 1);
+    return PointRec<double>{a.x, a.y, b.x, b.y};
+}
+__device__ __forceinline__ uint32_t rec_index(const PointRec<float>& r) { return __float_as_uint(r.w); }
+__device__ __forceinline__ uint32_t rec_index(const PointRec<double>& r) {
+    return uint32_t(__double_as_longlong(r.w));
+}
+
+template <typename T, int D>
+__device__ __forceinline__ T sqdist(const T (&q)[D], const PointRec<T>& p) {
+    const T d0 = sub_rn(q[0], p.x);
+    T acc = mul_rn(d0, d0);
+    if (D > 1) {
+        const T d1 = sub_rn(q[1], p.y);
+        acc = add_rn(acc, mul_rn(d1, d1));
+    }
+    if (D > 2) {
+        const T d2 = sub_rn(q[2], p.z);
+        acc = add_rn(acc, mul_rn(d2, d2));
+    }
+    return acc;
+}
+
+// ------------------------------------------------------------------ keys --
+
+template <typename T>
+struct Key;
+
+// f32: (distance bits << 32) | index.  Distances are >= +0, so their bit
+// patterns order like the values; NaN (0x7fc...) sorts above +inf.
+template <>
+struct Key<float> {
+    unsigned long long v;
+    static __device__ __forceinline__ Key make(float d, uint32_t i) {
+        return Key{(static_cast<unsigned long long>(__float_as_uint(d)) << 32) | i};
+    }
+    // worst possible real entry: +inf distance, index 2^32-1
+    static __device__ __forceinline__ Key sentinel() { return Key{0x7F800000FFFFFFFFull}; }
+    // front padding below every real key (see the top-k list below)
+    static __device__ __forceinline__ Key pad() { return Key{0ull}; }
+    __device__ __forceinline__ float dist() const { return __uint_as_float(uint32_t(v >> 32)); }
+    __device__ __forceinline__ uint32_t index() const { return uint32_t(v); }
+    __device__ __forceinline__ bool le(const Key& o) const { return v <= o.v; }
+    __device__ __forceinline__ bool lt(const Key& o) const { return v < o.v; }
+    __device__ __forceinline__ Key shfl(unsigned mask, int src, int width) const {
+        return Key{__shfl_sync(mask, v, src, width)};
+    }
+    __device__ __forceinline__ Key shfl_up(unsigned mask, int delta, int width) const {
+        return Key{__shfl_up_sync(mask, v, delta, width)};
+    }
+    __device__ __forceinline__ Key select(bool c, const Key& o) const { return c ? *this : o; }
+};
+
+// f64: distance bits and index side by side, compared lexicographically.
+template <>
+struct Key<double> {
+    unsigned long long d;
+    uint32_t i;
+    static __device__ __forceinline__ Key make(double dist, uint32_t idx) {
+        return Key{static_cast<unsigned long long>(__double_as_longlong(dist)), idx};
+    }
+    static __device__ __forceinline__ Key sentinel() { return Key{0x7FF0000000000000ull, 0xFFFFFFFFu}; }
+    static __device__ __forceinline__ Key pad() { return Key{0ull, 0u}; }
+    __device__ __forceinline__ double dist() const { return __longlong_as_double((long long)d); }
+    __device__ __forceinline__ uint32_t index() const { return i; }
+    __device__ __forceinline__ bool le(const Key& o) const { return d < o.d || (d == o.d && i <= o.i); }
+    __device__ __forceinline__ bool lt(const Key& o) const { return d < o.d || (d == o.d && i < o.i); }
+    __device__ __forceinline__ Key shfl(unsigned mask, int src, int width) const {
+        return Key{__shfl_sync(mask, d, src, width), __shfl_sync(mask, i, src, width)};
+    }
+    __device__ __forceinline__ Key shfl_up(unsigned mask, int delta, int width) const {
+        return Key{__shfl_up_sync(mask, d, delta, width), __shfl_up_sync(mask, i, delta, width)};
+    }
+    __device__ __forceinline__ Key select(bool c, const Key& o) const { return c ? *this : o; }
+};
+
+// ------------------------------------------------------------ top-k list --
+//
+// A sorted list of KMAX = G * R keys held in registers by a group of G lanes:
+// slot s lives on lane s % G, register s / G.  For a query asking for k <= KMAX
+// neighbours the first KMAX - k slots hold pad() (below every real key) and
+// the rest start at sentinel(); inserting a candidate c shifts every slot
+// above c one place up and drops the last, so the worst kept entry is always
+// slot KMAX - 1 (lane G-1, register R-1) and pads never move.  With G == 1 the
+// list is an ordinary per-thread register array.
+template <typename T, int G, int R>
+struct TopK {
+    Key<T> slot[R];
+
+    __device__ __forceinline__ void init(int k, int gl) {
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const int s = r * G + gl;
+            slot[r] = (s < G * R - k) ? Key<T>::pad() : Key<T>::sentinel();
+        }
+    }
+
+    // Insert c (the same value on every lane of the group).  gmask: the
+    // group's lanes; gl: this lane's rank in the group.
+    __device__ __forceinline__ void insert(const Key<T>& c, unsigned gmask, int gl) {
+        Key<T> nw[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const Key<T> old = slot[r];
+            Key<T> prev;
+            bool has_prev;
+            if (G == 1) {
+                prev = r > 0 ? slot[r - 1] : Key<T>::pad();
+                has_prev = r > 0;
+            } else {
+                const Key<T> up = old.shfl_up(gmask, 1, G);
+                const Key<T> wrap = r > 0 ? slot[r - 1].shfl(gmask, G - 1, G) : Key<T>::pad();
+                prev = gl == 0 ? wrap : up;
+                has_prev = !(gl == 0 && r == 0);
+            }
+            const bool keep = old.le(c);
+            const bool take = !has_prev || prev.le(c);
+            nw[r] = keep ? old : (take ? c : prev);
+        }
+#pragma unroll
+        for (int r = 0; r < R; ++r) slot[r] = nw[r];
+    }
+
+    __device__ __forceinline__ Key<T> worst(unsigned gmask) const {
+        if (G == 1) return slot[R - 1];
+        return slot[R - 1].shfl(gmask, G - 1, G);
+    }
+
+    // Write the k live slots of this lane to row `row` of the outputs.
+    __device__ __forceinline__ void store(int k, int gl, T* out_d, int32_t* out_i, long long row) const {
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const int s = r * G + gl;
+            const int o = s - (G * R - k);
+            if (o >= 0) {
+                out_d[row * k + o] = slot[r].dist();
+                out_i[row * k + o] = int32_t(slot[r].index());
+            }
+        }
+    }
+};
+
+// Offer the candidates of a group (one per lane; sentinel() when a lane has
+// none) to the group's list, in lane order.  Returns the new worst key.
+template <typename T, int G, int R>
+__device__ __forceinline__ Key<T> offer(TopK<T, G, R>& list, const Key<T>& mine, Key<T> worst,
+                                        unsigned gmask, int gl, int gbase) {
+    if (G == 1) {
+        if (mine.lt(worst)) {
+            list.insert(mine, gmask, gl);
+            worst = list.worst(gmask);
+        }
+        return worst;
+    }
+    unsigned m = __ballot_sync(gmask, mine.lt(worst));
+    if constexpr (G < 32) m = (m >> gbase) & ((1u << G) - 1u);
+    while (m) {
+        const int src = __ffs(m) - 1;
+        m &= m - 1;
+        const Key<T> c = mine.shfl(gmask, src, G);
+        if (c.lt(worst)) {
+            list.insert(c, gmask, gl);
+            worst = list.worst(gmask);
+        }
+    }
+    return worst;
+}
+
+template <int G>
+__device__ __forceinline__ unsigned group_mask(int lane) {
+    if constexpr (G == 32) {
+        return 0xFFFFFFFFu;
+    } else {
+        const int gbase = lane & ~(G - 1);
+        return ((1u << G) - 1u) << gbase;
+    }
+}
+
+}  // namespace tk

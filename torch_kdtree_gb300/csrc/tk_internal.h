@@ -1,0 +1,55 @@
+// Internal host-side declarations shared by the library's translation units.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/tk_knn.h"
+
+namespace tk {
+
+constexpr int kMaxLevels = 24;   // 2^24 leaves; the stack of a traversal holds <= kMaxLevels entries
+constexpr int kMaxK = 128;       // reference GPU cap (src/kdtree_g.cu:283,421)
+constexpr int kMaxBinLevels = 16;
+
+// Sets the thread-local error text and returns the status.
+int fail(int status, const std::string& msg);
+void clear_error();
+
+// Host copy of a tree in the reference's layout (src/kdtree.hpp:126-217) plus
+// the device image used by the kernels.
+template <typename T>
+struct HostTree {
+    int64_t n = 0;
+    int dims = 0;
+    int levels = 0;
+    std::vector<T> structured;        // [n*dims] points in leaf order
+    std::vector<int32_t> perm;        // [n] original index of structured point i
+    std::vector<T> medians;           // [2^L - 1] heap order; axis = depth % dims
+    std::vector<int32_t> leaf_off;    // [2^L + 1] prefix offsets of the leaves
+};
+
+// Builds the tree (tree_build.cpp).  Returns TK_OK or sets the error.
+template <typename T>
+int build_host_tree(const T* pts, int64_t n, int dims, int levels, int n_threads, HostTree<T>& out);
+
+}  // namespace tk
+
+// Opaque handle behind the C ABI.
+struct tk_tree {
+    int dtype = TK_F32;
+    int dims = 0;
+    int levels = 0;
+    int device = 0;
+    int64_t n = 0;
+    // host layout (one of the two is filled)
+    tk::HostTree<float> h32;
+    tk::HostTree<double> h64;
+    // device image
+    void* d_pts = nullptr;       // point records: coordinates + original index (see tk_device.cuh)
+    void* d_medians = nullptr;   // T[2^L - 1]
+    int32_t* d_leaf_off = nullptr;  // int32[2^L + 1]
+    int64_t device_bytes = 0;
+};

@@ -1,0 +1,146 @@
+// Host KD-tree construction in the reference's layout.
+//
+// Semantics of createKDTree / createPartitionRecursive / compMedian
+// (src/kdtree.hpp:392-534):
+//   * node at depth t splits on axis t % dims;
+//   * the node's points, ordered along that axis, go first floor(n/2) to the
+//     left child and the rest to the right child;
+//   * split value = middle element (odd n) or 0.5 * (a + b) of the two middle
+//     elements (even n), a + b rounded in T, the product taken in double;
+//   * heap numbering 2i+1 / 2i+2; leaves numbered left to right, stored
+//     contiguously; inside a leaf the points are ordered along the leaf
+//     parent's axis;
+//   * a split node that receives no point is an error.
+// The reference sorts the whole range at every level (O(N log^2 N)); here
+// upper levels use a linear-time selection and only leaf parents sort, which
+// yields the same layout for tie-free coordinates.  Ties on a coordinate are
+// ordered by original index (the reference's std::sort leaves them in an
+// unspecified order).  Subtrees are built in parallel threads.
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <thread>
+
+#include "tk_internal.h"
+
+namespace tk {
+namespace {
+
+template <typename T>
+struct Rec {
+    T c[3];
+    int32_t orig;
+};
+
+template <typename T>
+struct Builder {
+    int dims;
+    int levels;
+    int32_t nparts;
+    Rec<T>* recs;
+    T* medians;
+    int32_t* leaf_off;
+    std::atomic<bool> failed{false};  // set by any worker that meets an empty split node
+
+    static bool less(const Rec<T>& a, const Rec<T>& b, int ax) {
+        if (a.c[ax] < b.c[ax]) return true;
+        if (b.c[ax] < a.c[ax]) return false;
+        return a.orig < b.orig;
+    }
+
+    // compMedian (src/kdtree.hpp:392-401) on the values at ranks h-1 and h.
+    static T median_of(T lower_mid, T upper_mid, int32_t n) {
+        if (n % 2 == 1) return upper_mid;
+        const T s = lower_mid + upper_mid;  // rounded in T
+        return static_cast<T>(0.5 * static_cast<double>(s));
+    }
+
+    void node(int32_t lo, int32_t n, int32_t id, int depth, int spawn_depth) {
+        if (n == 0) {
+            failed.store(true);
+            return;
+        }
+        const int ax = depth % dims;
+        Rec<T>* r = recs + lo;
+        const int32_t h = n / 2;
+        auto cmp = [ax](const Rec<T>& a, const Rec<T>& b) { return less(a, b, ax); };
+        if (depth == levels - 1) {
+            std::sort(r, r + n, cmp);
+            medians[id] = median_of(h > 0 ? r[h - 1].c[ax] : r[h].c[ax], r[h].c[ax], n);
+            const int32_t leaf = 2 * id + 1 - nparts;
+            leaf_off[leaf] = lo;
+            leaf_off[leaf + 1] = lo + h;
+            return;
+        }
+        std::nth_element(r, r + h, r + n, cmp);
+        T lower_mid = r[h].c[ax];
+        if (h > 0) lower_mid = std::max_element(r, r + h, cmp)->c[ax];
+        medians[id] = median_of(lower_mid, r[h].c[ax], n);
+        if (depth < spawn_depth && n > 65536) {
+            std::thread left([=] { node(lo, h, 2 * id + 1, depth + 1, spawn_depth); });
+            node(lo + h, n - h, 2 * id + 2, depth + 1, spawn_depth);
+            left.join();
+        } else {
+            node(lo, h, 2 * id + 1, depth + 1, spawn_depth);
+            node(lo + h, n - h, 2 * id + 2, depth + 1, spawn_depth);
+        }
+    }
+};
+
+}  // namespace
+
+template <typename T>
+int build_host_tree(const T* pts, int64_t n, int dims, int levels, int n_threads, HostTree<T>& out) {
+    if (pts == nullptr) return fail(TK_EINVAL, "points pointer is null");
+    if (dims < 1 || dims > 3)
+        return fail(TK_EINVAL, "KD-tree supports dims 1, 2 or 3 (got " + std::to_string(dims) + ")");
+    if (n < 1) return fail(TK_EINVAL, "the reference point cloud is empty");
+    if (n >= (int64_t(1) << 31)) return fail(TK_EINVAL, "only 32 bit signed indexing implemented (n < 2^31)");
+    if (levels < 1 || levels > kMaxLevels)
+        return fail(TK_EINVAL, "levels must be in [1, " + std::to_string(kMaxLevels) + "]");
+    for (int64_t i = 0; i < n * dims; ++i)
+        if (std::isnan(pts[i])) return fail(TK_EINVAL, "reference points contain NaN");
+
+    const int32_t nparts = int32_t((1u << levels) - 1u);
+    std::vector<Rec<T>> recs(static_cast<size_t>(n));
+    for (int64_t i = 0; i < n; ++i) {
+        for (int c = 0; c < 3; ++c) recs[i].c[c] = c < dims ? pts[i * dims + c] : T(0);
+        recs[i].orig = int32_t(i);
+    }
+    out.n = n;
+    out.dims = dims;
+    out.levels = levels;
+    out.medians.assign(static_cast<size_t>(nparts), T(0));
+    out.leaf_off.assign(static_cast<size_t>(nparts) + 2, 0);
+
+    if (n_threads <= 0) n_threads = int(std::max(1u, std::thread::hardware_concurrency()));
+    int spawn_depth = 0;
+    while ((1 << spawn_depth) < n_threads && spawn_depth < 8) ++spawn_depth;
+
+    Builder<T> b;
+    b.dims = dims;
+    b.levels = levels;
+    b.nparts = nparts;
+    b.recs = recs.data();
+    b.medians = out.medians.data();
+    b.leaf_off = out.leaf_off.data();
+    b.node(0, int32_t(n), 0, 0, spawn_depth);
+    if (b.failed.load())
+        return fail(TK_EINVAL,
+                    "Ran out of points while building KD-Tree. Either you required too many levels, "
+                    "or you used a lot of coplanar points");
+    out.leaf_off.resize(static_cast<size_t>(nparts) + 2);
+    out.leaf_off[nparts + 1] = int32_t(n);  // 2^L leaves -> 2^L + 1 offsets
+    out.structured.resize(static_cast<size_t>(n) * dims);
+    out.perm.resize(static_cast<size_t>(n));
+    for (int64_t i = 0; i < n; ++i) {
+        for (int c = 0; c < dims; ++c) out.structured[i * dims + c] = recs[i].c[c];
+        out.perm[i] = recs[i].orig;
+    }
+    return TK_OK;
+}
+
+template int build_host_tree<float>(const float*, int64_t, int, int, int, HostTree<float>&);
+template int build_host_tree<double>(const double*, int64_t, int, int, int, HostTree<double>&);
+
+}  // namespace tk

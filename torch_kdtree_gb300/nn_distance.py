@@ -1,0 +1,209 @@
+"""Python API of the engine, mirroring torch_kdtree's (torch_kdtree/nn_distance.py).
+
+    tree = build_kd_tree(points_ref)                 # KD-tree built on the host, uploaded once
+    dists, inds = tree.query(points_query, nr_nns_searches=k)
+
+Same names, argument meaning and error behaviour as the reference:
+``build_kd_tree(points_ref, device=None, squared_distances=True, levels=None)``
+and ``TorchKDTree.query(points_query, nr_nns_searches=1, result_dists=None,
+result_idx=None)``.  Differences, all deliberate:
+
+* ``inds`` are int32 original indices computed on the GPU (the reference
+  returned ``shuffled_ind[result_idx].long()``, int64); ``inds.long()`` gives
+  the reference's dtype.
+* among neighbours at exactly equal distance the lower original index wins
+  (the reference kept the first one its traversal visited);
+* gradients flow through a hand-written, deterministic backward kernel
+  instead of torch indexing with atomics;
+* ``levels`` may exceed 13 (the reference's limit came from its kernel's
+  shared-memory visit tags), up to 24;
+* only CUDA trees: this engine has no CPU query implementation.
+"""
+from __future__ import annotations
+
+import ctypes
+from typing import Optional, Union
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import LIB, QueryOpts, TreeInfo, check
+
+gpu_available = bool(torch.cuda.is_available() and LIB.tk_cuda_available())
+
+_DTYPES = {torch.float32: _lib.TK_F32, torch.float64: _lib.TK_F64}
+MAX_LEVELS = 24
+MAX_K = 128
+
+
+def default_levels(n: int) -> int:
+    """The reference's heuristic: max(1, min(13, floor(log2 n) - 3))
+    (torch_kdtree/nn_distance.py:146-147)."""
+    return int(np.maximum(1, np.minimum(13, int(np.log(int(n)) / np.log(2)) - 3)))
+
+
+def _stream_ptr(device: torch.device) -> int:
+    return torch.cuda.current_stream(device).cuda_stream
+
+
+def _workspace(nbytes: int, device: torch.device) -> torch.Tensor:
+    return torch.empty(max(int(nbytes), 1), dtype=torch.uint8, device=device)
+
+
+class _Tree:
+    """Owner of a tk_tree handle."""
+
+    def __init__(self, points: np.ndarray, levels: int, device_index: int):
+        n, d = points.shape
+        dt = _lib.TK_F32 if points.dtype == np.float32 else _lib.TK_F64
+        h = ctypes.c_void_p()
+        check(LIB.tk_tree_create(points.ctypes.data, n, d, dt, levels, device_index, 0, ctypes.byref(h)))
+        self.handle = h
+
+    def info(self) -> TreeInfo:
+        info = TreeInfo()
+        check(LIB.tk_tree_get_info(self.handle, ctypes.byref(info)))
+        return info
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h is not None and h.value:
+            LIB.tk_tree_destroy(h)
+            self.handle = None
+
+
+def knn_query_raw(tree: _Tree, q: torch.Tensor, k: int, dists: torch.Tensor, idx: torch.Tensor,
+                  opts: Optional[QueryOpts] = None) -> None:
+    """Enqueue one tk_tree_query on the current stream (inputs already on the device)."""
+    nq = q.shape[0]
+    ws_bytes = LIB.tk_tree_query_workspace_size(tree.handle, nq)
+    ws = _workspace(ws_bytes, q.device)
+    check(LIB.tk_tree_query(tree.handle, q.data_ptr(), nq, k, dists.data_ptr(), idx.data_ptr(),
+                            ctypes.byref(opts) if opts is not None else None, ws.data_ptr(), ws_bytes,
+                            _stream_ptr(q.device)))
+
+
+class TorchKDTree:
+    def __init__(self, points_ref: torch.Tensor, device: torch.device, levels: int, squared_distances: bool,
+                 query_opts: Optional[QueryOpts] = None):
+        """Builds the KD-tree.  See :func:`build_kd_tree`."""
+        if device.type != "cuda":
+            raise RuntimeError(
+                "Could not find the KD-Tree for your specified options: this engine builds CUDA trees only "
+                f"(requested device {device}).")
+        if points_ref.shape[0] >= 2 ** 31:
+            raise AssertionError("Only 32 bit signed indexing implemented")
+        self.dtype = points_ref.dtype
+        self.dims = points_ref.shape[-1]
+        self.nr_ref_points = points_ref.shape[0]
+        if points_ref.dim() != 2 or self.dtype not in _DTYPES or self.dims not in (1, 2, 3):
+            raise RuntimeError(
+                "Could not find the KD-Tree for your specified options. This probably means the library was not "
+                f"compiled for the specified dimensionality ({self.dims}) or precision ({self.dtype}).")
+        if device.index is None:
+            device = torch.device("cuda", torch.cuda.current_device())
+        self.device = device
+        self.levels = int(levels)
+        host = np.ascontiguousarray(points_ref.detach().cpu().numpy())
+        self._tree = _Tree(host, self.levels, device.index)
+        self.dtype_idx = torch.int32
+        self.ref_requires_grad = points_ref.requires_grad
+        self.points_ref_bak = points_ref
+        self.squared_distances = squared_distances
+        self.use_gpu = True
+        self.query_opts = query_opts
+        self._structured = None
+        self._shuffled = None
+
+    # Layout, as the reference exposes it (torch_kdtree/nn_distance.py:30-41)
+    @property
+    def structured_points(self) -> torch.Tensor:
+        if self._structured is None:
+            out = np.empty((self.nr_ref_points, self.dims), dtype=np.float32 if self.dtype == torch.float32
+                           else np.float64)
+            check(LIB.tk_tree_get_points(self._tree.handle, out.ctypes.data))
+            self._structured = torch.from_numpy(out).to(self.device)
+        return self._structured
+
+    @property
+    def shuffled_ind(self) -> torch.Tensor:
+        if self._shuffled is None:
+            out = np.empty(self.nr_ref_points, dtype=np.int32)
+            check(LIB.tk_tree_get_perm(self._tree.handle, out.ctypes.data))
+            self._shuffled = torch.from_numpy(out).long().to(self.device)
+        return self._shuffled
+
+    def query(self, points_query: torch.Tensor, nr_nns_searches: int = 1,
+              result_dists: Optional[torch.Tensor] = None, result_idx: Optional[torch.Tensor] = None):
+        """Exact KNN of ``points_query`` in the tree.
+
+        Returns ``(dists, inds)``: squared (or, with ``squared_distances=False``,
+        plain) distances ``[Q, k]`` in the tree's dtype and int32 original
+        indices ``[Q, k]``.  Raises RuntimeError when k exceeds the number of
+        points, AssertionError on dtype / shape mismatches, as the reference."""
+        k = int(nr_nns_searches)
+        if k > self.nr_ref_points:
+            raise RuntimeError("You requested more nearest neighbors than there are in the KD-Tree")
+        if k < 1:
+            raise RuntimeError("nr_nns_searches must be at least 1")
+        if k > MAX_K:
+            raise RuntimeError(f"nr_nns_searches is limited to {MAX_K} on the GPU")
+        points_query = points_query.to(self.device)
+        nq = points_query.shape[0]
+        if result_dists is None:
+            result_dists = torch.empty((nq, k), dtype=self.dtype, device=self.device)
+        if result_idx is None:
+            result_idx = torch.empty((nq, k), dtype=self.dtype_idx, device=self.device)
+        if list(result_dists.shape) != [nq, k] or result_dists.dtype != self.dtype:
+            raise AssertionError("result_dists must be [Q, k] of the tree's dtype")
+        if list(result_idx.shape) != [nq, k] or result_idx.dtype != self.dtype_idx:
+            raise AssertionError("result_idx must be [Q, k] int32")
+        if points_query.dtype != self.dtype:
+            raise AssertionError(f"points_query has dtype {points_query.dtype}, the tree {self.dtype}")
+        if points_query.dim() != 2 or points_query.shape[1] != self.dims:
+            raise AssertionError(f"points_query must be [Q, {self.dims}]")
+        if not result_dists.is_contiguous():
+            result_dists = result_dists.contiguous()
+        if not result_idx.is_contiguous():
+            result_idx = result_idx.contiguous()
+        if not points_query.is_contiguous():
+            points_query = points_query.contiguous()
+
+        need_grad = torch.is_grad_enabled() and (points_query.requires_grad or self.ref_requires_grad)
+        if need_grad:
+            from .autograd import KnnDistances
+            ref = self.points_ref_bak.to(self.device)
+            dists, inds = KnnDistances.apply(points_query, ref, self, k)
+            with torch.no_grad():
+                result_dists.copy_(dists)
+                result_idx.copy_(inds)
+        else:
+            knn_query_raw(self._tree, points_query.detach(), k, result_dists, result_idx, self.query_opts)
+            dists, inds = result_dists, result_idx
+        if not self.squared_distances:
+            dists = torch.sqrt(dists)
+        return dists, inds
+
+
+def build_kd_tree(points_ref: Union[torch.Tensor, np.ndarray], device: Optional[torch.device] = None,
+                  squared_distances: bool = True, levels: Optional[int] = None,
+                  query_opts: Optional[QueryOpts] = None) -> TorchKDTree:
+    """Builds the KD-tree for subsequent queries (torch_kdtree/nn_distance.py:119-160).
+
+    The tree is built on the host in the reference's layout and uploaded once.
+    ``device`` defaults to ``points_ref.device`` (which must then be CUDA);
+    ``levels`` defaults to the reference's heuristic and may range 1..24."""
+    if issubclass(type(points_ref), np.ndarray):
+        points_ref = torch.from_numpy(points_ref)
+    if device is None:
+        device = points_ref.device
+    if levels is None:
+        levels = default_levels(points_ref.shape[0])
+    if issubclass(type(device), str):
+        device = torch.device(device)
+    assert 1 <= levels <= MAX_LEVELS, f"levels must be in [1, {MAX_LEVELS}]"
+    assert issubclass(type(points_ref), torch.Tensor)
+    assert device.type != "cuda" or gpu_available, "You requested the KD-Tree on the GPU, but no CUDA device is visible"
+    assert device.type in ["cuda", "cpu"]
+    return TorchKDTree(points_ref, device, levels, squared_distances, query_opts)
