@@ -204,13 +204,27 @@ def run_ours(args, rank, world):
     t0 = time.perf_counter()
     plain = tk.build_kd_tree(ref)
     build_plain_s = time.perf_counter() - t0
-    # ---- chosen: autotuned depth and lanes per query
+    # ---- chosen: autotuned depth and lanes per query (or given on the command line)
     t0 = time.perf_counter()
-    ch = autotune(ref, q, K_NN, use_cache=False)
+    if args.levels and args.tpq:
+        from torch_kdtree_gb300.autotune import Choice
+        ch = Choice(levels=args.levels, threads_per_query=args.tpq, ms=float("nan"), plain_levels=plain.levels,
+                    table=[])
+    else:
+        ch = autotune(ref, q, K_NN, use_cache=False)
     tune_s = time.perf_counter() - t0
     t0 = time.perf_counter()
     chosen = tk.build_kd_tree(ref, levels=ch.levels, query_opts=QueryOpts.make(threads_per_query=ch.threads_per_query))
     build_chosen_s = time.perf_counter() - t0
+
+    if args.profile:
+        # one query of each tree, nothing else (for ncu captures)
+        for tree in (chosen, plain):
+            dd = torch.empty(nq, K_NN, device=dev)
+            ii = torch.empty(nq, K_NN, dtype=torch.int32, device=dev)
+            knn_query_raw(tree._tree, q, K_NN, dd, ii, tree.query_opts)
+        torch.cuda.synchronize()
+        return
 
     d_plain = torch.empty(nq, K_NN, device=dev)
     i_plain = torch.empty(nq, K_NN, dtype=torch.int32, device=dev)
@@ -368,6 +382,152 @@ def cpu_baseline(ref_np, q_np, gpu_idx, gpu_d, sample):
              "dist_bit_mismatches": cmp.dist_bit_mismatch}
     return cpu, exact
 
+# ------------------------------------------------------ other workloads --
+
+def _event_ms(fn, steps, warmup, flush=None):
+    import torch
+    for _ in range(warmup):
+        if flush is not None:
+            flush.zero_()
+        fn()
+    torch.cuda.synchronize()
+    ms = []
+    for _ in range(steps):
+        if flush is not None:
+            flush.zero_()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record()
+        fn()
+        b.record()
+        b.synchronize()
+        ms.append(a.elapsed_time(b))
+    return ms
+
+
+def run_batched(args):
+    """256 ragged clouds (sizes log-uniform in [1e3, 2e5], 8-Gaussian
+    mixtures, queries = half the size, k from {1, 4, 16}): one graph-captured
+    persistent launch vs one launch per cloud."""
+    import torch
+
+    from torch_kdtree_gb300.batched import BatchedKDTrees
+    from torch_kdtree_gb300.synthetic import ragged_clouds
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    clouds = ragged_clouds(n_clouds=256, seed=0)
+    refs = [torch.from_numpy(r).to(dev) for r, _, _ in clouds]
+    qs = [torch.from_numpy(q).to(dev) for _, q, _ in clouds]
+    ks = [k for _, _, k in clouds]
+    qc = [q.shape[0] for q in qs]
+    q_flat = torch.cat(qs).contiguous()
+    total_q = q_flat.shape[0]
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    leaf = args.leaf_size
+    tuned_levels = [int(max(1, min(24, round(np.log2(max(2, len(r)) / leaf))))) for r, _, _ in clouds]
+    t0 = time.perf_counter()
+    plain = BatchedKDTrees(refs, ks, qc)  # reference heuristic depth per cloud
+    tuned = BatchedKDTrees(refs, ks, qc, levels=tuned_levels)
+    build_s = time.perf_counter() - t0
+    ms_plain = _event_ms(lambda: plain.query_each(qs), args.steps, args.warmup, flush)
+    ms_each_tuned = _event_ms(lambda: tuned.query_each(qs), args.steps, args.warmup, flush)
+    replay = tuned.graph(q_flat)
+    ms_batch = _event_ms(replay, args.steps, args.warmup, flush)
+    plain.query_each(qs)
+    replay()
+    torch.cuda.synchronize()
+    same = bool(torch.equal(plain.out_dists, tuned.out_dists) and torch.equal(plain.out_idx, tuned.out_idx))
+    t_b = sum(ms_batch) / 1e3
+    value = total_q * args.steps / t_b
+    line = {
+        "metric": "KNN queries/s, 256 ragged clouds (d=3, k in {1,4,16}), one graph-captured launch vs 256 plain launches",
+        "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * t_b / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded numpy mixtures)",
+        "config": {"workload": f"256 clouds, {sum(len(r) for r, _, _ in clouds)} ref points, {total_q} queries",
+                   "tuned_leaf_size": leaf, "l2": "flushed between steps", "tree_build_s": build_s},
+        "plain_256_launches": {"value": total_q * args.steps / (sum(ms_plain) / 1e3),
+                               "ms_per_step": sum(ms_plain) / args.steps},
+        "tuned_trees_256_launches": {"value": total_q * args.steps / (sum(ms_each_tuned) / 1e3),
+                                     "ms_per_step": sum(ms_each_tuned) / args.steps},
+        "batched_vs_plain": (sum(ms_plain) / sum(ms_batch)),
+        "identical_results": same,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_backward(args):
+    """Differentiable KNN: 1,048,576 refs and queries N(0,1), k=8, loss =
+    0.5 * sum(dists * w); forward query vs the hand-written backward."""
+    import torch
+
+    import torch_kdtree_gb300 as tk
+    from torch_kdtree_gb300._lib import QueryOpts
+    from torch_kdtree_gb300.autograd import knn_backward
+    from torch_kdtree_gb300.nn_distance import knn_query_raw
+    from torch_kdtree_gb300.synthetic import differentiable
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    ref_np, q_np, w_np = differentiable()
+    ref = torch.from_numpy(ref_np).to(dev)
+    q = torch.from_numpy(q_np).to(dev)
+    w = torch.from_numpy(w_np).to(dev)
+    k = 8
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    res = {}
+    for name, levels, tpq in (("plain", None, 0), ("chosen", args.levels or 16, args.tpq or 1)):
+        tree = tk.build_kd_tree(ref, levels=levels, query_opts=QueryOpts.make(threads_per_query=tpq))
+        d = torch.empty(len(q), k, device=dev)
+        i = torch.empty(len(q), k, dtype=torch.int32, device=dev)
+        fwd = _event_ms(lambda: knn_query_raw(tree._tree, q, k, d, i, tree.query_opts), args.steps, args.warmup,
+                        flush)
+        g = 0.5 * w
+        bwd = _event_ms(lambda: knn_backward(q, ref, i, g, True, True), args.steps, args.warmup, flush)
+        res[name] = {"levels": tree.levels, "forward_ms": sum(fwd) / len(fwd), "backward_ms": sum(bwd) / len(bwd)}
+        res[name]["backward_over_forward"] = res[name]["backward_ms"] / res[name]["forward_ms"]
+    line = {
+        "metric": "backward time / forward time, differentiable KNN (1M refs, 1M queries, d=3, k=8)",
+        "value": res["chosen"]["backward_over_forward"], "unit": "ratio", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": res["chosen"]["backward_ms"], "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded numpy)",
+        "config": {"workload": "1,048,576 refs + 1,048,576 queries N(0,1), k=8, w U(0,1)",
+                   "l2": "flushed between steps"},
+        "runs": res,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_brute(args):
+    """Brute-force nn_distance on the 65,536 x 65,536 subset of the large
+    workload, k = 1, float32 CUDA cores, the reference's arithmetic."""
+    import torch
+
+    import torch_kdtree_gb300 as tk
+    from torch_kdtree_gb300.nn_distance import nn_distance_raw
+    from torch_kdtree_gb300.synthetic import cube_and_sphere
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    ref_np, q_np = cube_and_sphere()
+    ref = torch.from_numpy(ref_np[:65536]).to(dev)
+    q = torch.from_numpy(q_np[:65536]).to(dev)
+    d = torch.empty(65536, 1, device=dev)
+    i = torch.empty(65536, 1, dtype=torch.int32, device=dev)
+    ms = _event_ms(lambda: nn_distance_raw(ref, q, 1, d, i, "exact"), args.steps, args.warmup)
+    kd, ki = tk.build_kd_tree(ref).query(q, nr_nns_searches=1)
+    t = sum(ms) / len(ms) / 1e3
+    pairs = 65536 * 65536
+    line = {
+        "metric": "brute-force KNN pairs/s (65,536 x 65,536, d=3, k=1, float32 exact)",
+        "value": pairs / t, "unit": "pairs/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * t, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (first 65,536 refs and queries of the large workload)",
+        "config": {"workload": "nn_distance 65,536 x 65,536, k=1"},
+        "queries_per_s": 65536 / t, "gflops_2d_per_pair": 6 * pairs / t / 1e9,
+        "identical_to_kdtree": bool(torch.equal(kd, d) and torch.equal(ki, i)),
+    }
+    print(json.dumps(line), flush=True)
+
+
 
 def main():
     p = argparse.ArgumentParser()
@@ -377,6 +537,13 @@ def main():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--ref-sample", type=int, default=131072)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--levels", type=int, default=0, help="chosen tree depth (skips the autotuner with --tpq)")
+    p.add_argument("--tpq", type=int, default=0, help="chosen lanes per query (skips the autotuner with --levels)")
+    p.add_argument("--profile", action="store_true", help="run one chosen and one plain query only (for ncu)")
+    p.add_argument("--workload", default="kd", choices=["kd", "batched", "backward", "brute"],
+                   help="kd (default): the headline large single-cloud query; the others measure the "
+                        "batched, backward and brute-force paths")
+    p.add_argument("--leaf-size", type=int, default=16, help="target points per leaf of tuned batch trees")
     args = p.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     world = env_int("WORLD_SIZE", 1)
@@ -384,6 +551,10 @@ def main():
     if args.impl == "reference":
         if rank == 0:
             run_reference(args)
+        return
+    if args.workload != "kd":
+        if rank == 0:
+            {"batched": run_batched, "backward": run_backward, "brute": run_brute}[args.workload](args)
         return
     if world > 1:
         import torch

@@ -110,6 +110,51 @@ size_t tk_tree_query_workspace_size(const tk_tree* tree, int64_t nq);
 int tk_tree_query(const tk_tree* tree, const void* q, int64_t nq, int k, void* dists, int32_t* idx,
                   const tk_query_opts* opts, void* workspace, size_t workspace_bytes, void* stream);
 
+/* ------------------------------------------------------------ batches -- */
+
+typedef struct tk_batch tk_batch;
+
+/* Plan a batched query over n_trees clouds, each with its own tree (same
+ * dtype, dims and device) and its own k (ks[c], 1..min(n_c, 128)); query
+ * counts per cloud are fixed by q_counts.  The trees must outlive the batch.
+ * Queries are passed concatenated cloud after cloud ([sum q_counts, dims]);
+ * results come back concatenated the same way, cloud c occupying a
+ * [q_counts[c], ks[c]] block.  No reference counterpart: the reference
+ * queried one cloud per call (src/interface.cpp:79-86). */
+int tk_batch_create(const tk_tree* const* trees, int n_trees, const int64_t* q_counts, const int32_t* ks,
+                    tk_batch** out);
+int tk_batch_destroy(tk_batch* batch);
+size_t tk_batch_workspace_size(const tk_batch* batch);
+/* Number of output elements (sum of q_counts[c] * ks[c]). */
+int64_t tk_batch_output_size(const tk_batch* batch);
+/* All clouds in one persistent launch fed by a global work counter (plus
+ * the binning kernels).  Device work only, no host synchronisation and no
+ * allocation: it can be captured in a CUDA graph.  threads_per_query: 0 =
+ * auto, 1 (max k <= 16) or 8. */
+int tk_batch_query(const tk_batch* batch, const void* q, void* dists, int32_t* idx, int threads_per_query,
+                   void* workspace, size_t workspace_bytes, void* stream);
+
+/* -------------------------------------------------------- brute force -- */
+
+typedef enum tk_brute_mode {
+    TK_BRUTE_EXACT = 0,      /* CUDA cores, the reference's distance arithmetic (float or double) */
+    TK_BRUTE_TF32 = 1,       /* q.r on tensor cores in TF32, over-fetch, exact FP32 re-rank */
+    TK_BRUTE_BF16_SPLIT = 2  /* q.r as BF16 hi/lo split products with FP32 accumulation, then exact re-rank */
+} tk_brute_mode;
+
+/* Bytes of device scratch tk_nn_distance needs. */
+size_t tk_nn_distance_workspace_size(int64_t n, int64_t nq, int dims, int k, int dtype, int mode);
+
+/* Exhaustive exact k nearest neighbours (the nn_distance op).
+ * ref: device [n, dims]; q: device [nq, dims]; dists [nq, k] squared
+ * distances, idx int32 [nq, k]; 1 <= dims <= 128 (float64: dims <= 4),
+ * 1 <= k <= min(n, 128).  Every mode returns the same answer as the KD-tree
+ * query: ordered by (distance computed as the reference does, index).
+ * Replaces NmDistanceKernelLauncherDynamic (src/nndistance_g.cu:191-220),
+ * which had no Python binding, ran one thread block and only d = 3. */
+int tk_nn_distance(const void* ref, int64_t n, const void* q, int64_t nq, int dims, int k, int dtype, int mode,
+                   void* dists, int32_t* idx, void* workspace, size_t workspace_bytes, void* stream);
+
 /* ----------------------------------------------------------- backward -- */
 
 /* Bytes of device scratch tk_knn_backward needs when grad_ref is requested. */
@@ -118,7 +163,7 @@ size_t tk_knn_backward_workspace_size(int64_t nq, int k, int64_t n);
 /* Gradient of squared KNN distances dist[i,j] = |q[i] - ref[idx[i,j]]|^2:
  *   grad_q[i]   = sum_j 2 g[i,j] (q[i] - ref[idx[i,j]])
  *   grad_ref[m] = sum over pairs with idx[i,j] == m of 2 g[i,j] (ref[m] - q[i])
- * q [nq,dims], ref [n,dims], idx int32 [nq,k] (original indices; entries
+ * q [nq,dims], ref [n,dims] (1 <= dims <= 128), idx int32 [nq,k] (original indices; entries
  * outside [0,n) are skipped), grad_dists [nq,k]; grad_q [nq,dims] and
  * grad_ref [n,dims] are overwritten; either may be NULL to skip it.  The ref
  * gradient is a stable-sort + fixed-order segmented reduction: bitwise

@@ -55,9 +55,9 @@ def test_backward_is_bitwise_deterministic():
         dists, _ = tk().build_kd_tree(r).query(qq, nr_nns_searches=8)
         (0.5 * (dists * w).sum()).backward()
         outs.append((qq.grad.clone(), r.grad.clone()))
-    for a, b in outs[1:]:
-        assert torch.equal(a[0], outs[0][0])
-        assert torch.equal(a[1], outs[0][1])
+    for gq, gr in outs[1:]:
+        assert torch.equal(gq, outs[0][0])
+        assert torch.equal(gr, outs[0][1])
 
 
 def test_finite_differences_fp64():

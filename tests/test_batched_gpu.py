@@ -1,0 +1,65 @@
+"""Batched ragged clouds in one persistent launch: identical, bit for bit,
+to one tree query per cloud, and to the oracle's exhaustive search."""
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+cuda = torch.device("cuda")
+
+
+def make_clouds(n_clouds, lo, hi, seed):
+    from torch_kdtree_gb300.synthetic import ragged_clouds
+    return ragged_clouds(n_clouds=n_clouds, lo=lo, hi=hi, seed=seed)
+
+
+@pytest.mark.parametrize("tpq", [0, 8])
+def test_batch_matches_per_cloud_and_oracle(tpq, oracle):
+    from torch_kdtree_gb300.batched import BatchedKDTrees
+    clouds = make_clouds(24, 50, 20000, seed=3)
+    refs = [torch.from_numpy(r).to(cuda) for r, _, _ in clouds]
+    qs = [torch.from_numpy(q).to(cuda) for _, q, _ in clouds]
+    ks = [k for _, _, k in clouds]
+    b = BatchedKDTrees(refs, ks, [q.shape[0] for q in qs], threads_per_query=tpq)
+    d_b, i_b = b.query(qs)
+    b.query_each(qs)
+    d_e, i_e = b.split(b.out_dists), b.split(b.out_idx)
+    for c, ((r, q, k), db, ib, de, ie) in enumerate(zip(clouds, d_b, i_b, d_e, i_e)):
+        assert torch.equal(db, de) and torch.equal(ib, ie), c
+        bd, bi = oracle.brute(r, q, k)
+        np.testing.assert_array_equal(db.cpu().numpy(), bd)
+        np.testing.assert_array_equal(ib.cpu().numpy(), bi)
+
+
+def test_batch_graph_replay_and_large_k(oracle):
+    from torch_kdtree_gb300.batched import BatchedKDTrees
+    rng = np.random.default_rng(9)
+    refs_np = [rng.standard_normal((n, 3)).astype(np.float32) for n in (300, 5000, 40000, 129)]
+    qs_np = [rng.standard_normal((n, 3)).astype(np.float32) for n in (0, 2500, 7000, 64)]
+    ks = [3, 100, 17, 128]
+    b = BatchedKDTrees([torch.from_numpy(r).to(cuda) for r in refs_np], ks, [len(q) for q in qs_np],
+                       levels=[2, None, 14, 1])
+    q_flat = torch.from_numpy(np.concatenate(qs_np)).to(cuda)
+    replay = b.graph(q_flat)
+    b.out_dists.fill_(-1)
+    replay()
+    torch.cuda.synchronize()
+    for (r, q, k, d, i) in zip(refs_np, qs_np, ks, b.split(b.out_dists), b.split(b.out_idx)):
+        if len(q) == 0:
+            continue
+        bd, bi = oracle.brute(r, q, k)
+        np.testing.assert_array_equal(d.cpu().numpy(), bd)
+        np.testing.assert_array_equal(i.cpu().numpy(), bi)
+
+
+def test_batch_errors():
+    from torch_kdtree_gb300.batched import BatchedKDTrees
+    r = torch.randn(10, 3, device=cuda)
+    with pytest.raises(Exception):
+        BatchedKDTrees([r], [11], [4])  # k > n
+    with pytest.raises(Exception):
+        BatchedKDTrees([r, torch.randn(10, 3, device=cuda, dtype=torch.float64)], [1, 1], [1, 1])
+    b = BatchedKDTrees([r], [2], [4])
+    with pytest.raises(Exception):
+        b.query_flat(torch.randn(5, 3, device=cuda))  # wrong query count

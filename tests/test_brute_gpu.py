@@ -1,0 +1,90 @@
+"""GPU parity of the exhaustive search (nn_distance, tk_nn_distance):
+bit-exact against the oracle's exhaustive search, and identical to the
+KD-tree query on the same inputs."""
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+cuda = torch.device("cuda")
+
+
+def tk():
+    import torch_kdtree_gb300
+    return torch_kdtree_gb300
+
+
+@pytest.mark.parametrize("d", [1, 2, 3, 4, 5, 8, 17, 32, 64, 128])
+@pytest.mark.parametrize("k", [1, 3, 16, 32, 100])
+def test_exact_mode_matches_oracle(d, k, oracle):
+    rng = np.random.default_rng(d * 1000 + k)
+    n = 6000 if d <= 32 else 3000
+    ref = rng.standard_normal((n, d)).astype(np.float32)
+    q = rng.standard_normal((700, d)).astype(np.float32)
+    dd, ii = tk().nn_distance(torch.from_numpy(ref).to(cuda), torch.from_numpy(q).to(cuda), k)
+    bd, bi = oracle.brute(ref, q, k)
+    np.testing.assert_array_equal(dd.cpu().numpy(), bd)
+    np.testing.assert_array_equal(ii.cpu().numpy(), bi)
+
+
+@pytest.mark.parametrize("d", [1, 2, 3])
+def test_float64(d, oracle):
+    rng = np.random.default_rng(40 + d)
+    ref = rng.standard_normal((5000, d))
+    q = rng.standard_normal((500, d))
+    dd, ii = tk().nn_distance(torch.from_numpy(ref).to(cuda), torch.from_numpy(q).to(cuda), 7)
+    bd, bi = oracle.brute(ref, q, 7)
+    np.testing.assert_array_equal(dd.cpu().numpy(), bd)
+    np.testing.assert_array_equal(ii.cpu().numpy(), bi)
+
+
+def test_brute_equals_kdtree():
+    g = torch.Generator().manual_seed(3)
+    ref = torch.rand(65536, 3, generator=g).to(cuda)
+    q = torch.rand(8192, 3, generator=g).to(cuda)
+    for k in (1, 16):
+        bd, bi = tk().nn_distance(ref, q, k)
+        kd, ki = tk().build_kd_tree(ref).query(q, nr_nns_searches=k)
+        assert torch.equal(bd, kd) and torch.equal(bi, ki)
+
+
+def test_duplicates_and_many_slices(oracle):
+    """5% exact duplicates; few queries so the reference set is sliced across
+    many blocks and the per-slice lists are merged."""
+    rng = np.random.default_rng(77)
+    ref = rng.standard_normal((200_000, 8)).astype(np.float32)
+    m = 10_000
+    perm = rng.permutation(len(ref))
+    ref[perm[:m]] = ref[perm[m:2 * m]]
+    q = ref[rng.integers(0, len(ref), 64)] + np.float32(0)
+    dd, ii = tk().nn_distance(torch.from_numpy(ref).to(cuda), torch.from_numpy(q).to(cuda), 32)
+    bd, bi = oracle.brute(ref, q, 32)
+    np.testing.assert_array_equal(dd.cpu().numpy(), bd)
+    np.testing.assert_array_equal(ii.cpu().numpy(), bi)
+
+
+def test_brute_backward_matches_torch():
+    g = torch.Generator().manual_seed(5)
+    for d in (3, 8, 32):
+        ref = torch.randn(4000, d, generator=g).to(cuda).requires_grad_(True)
+        q = torch.randn(3000, d, generator=g).to(cuda).requires_grad_(True)
+        w = torch.rand(3000, 4, generator=g).to(cuda)
+        dists, inds = tk().nn_distance(ref, q, 4)
+        (0.5 * (dists * w).sum()).backward()
+        q2 = q.detach().clone().requires_grad_(True)
+        r2 = ref.detach().clone().requires_grad_(True)
+        d2 = torch.sum((q2[:, None] - r2[inds.long()]) ** 2, -1)
+        (0.5 * (d2 * w).sum()).backward()
+        assert torch.allclose(q.grad, q2.grad, rtol=1e-4, atol=1e-4)
+        assert torch.allclose(ref.grad, r2.grad, rtol=1e-4, atol=1e-4)
+
+
+def test_errors():
+    ref = torch.randn(10, 3, device=cuda)
+    with pytest.raises(Exception):
+        tk().nn_distance(ref, torch.randn(4, 3, device=cuda), 11)
+    with pytest.raises(Exception):
+        tk().nn_distance(ref, torch.randn(4, 2, device=cuda), 1)
+    with pytest.raises(Exception):
+        tk().nn_distance(ref, torch.randn(4, 3, device=cuda, dtype=torch.float64), 1)

@@ -4,7 +4,7 @@
     tree = build_kd_tree(points_ref)            # on a CUDA device
     dists, inds = tree.query(points_query, nr_nns_searches=k)
 """
-from .nn_distance import TorchKDTree, build_kd_tree, default_levels, gpu_available
+from .nn_distance import TorchKDTree, build_kd_tree, default_levels, gpu_available, nn_distance
 
-__all__ = ["build_kd_tree", "gpu_available", "TorchKDTree", "default_levels"]
+__all__ = ["build_kd_tree", "gpu_available", "TorchKDTree", "default_levels", "nn_distance"]
 __version__ = "0.1.0"

@@ -20,6 +20,9 @@ TK_ECUDA = 5
 TK_EWORKSPACE = 6
 TK_F32 = 0
 TK_F64 = 1
+TK_BRUTE_EXACT = 0
+TK_BRUTE_TF32 = 1
+TK_BRUTE_BF16_SPLIT = 2
 
 _STATUS_NAMES = {
     TK_EINVAL: "EINVAL", TK_ENOMEM: "ENOMEM", TK_EUNSUPPORTED: "EUNSUPPORTED",
@@ -73,6 +76,14 @@ SIGNATURES = {
     "tk_tree_get_splits": (_int, [_vp, _vp, _vp]),
     "tk_tree_query_workspace_size": (_sz, [_vp, _i64]),
     "tk_tree_query": (_int, [_vp, _vp, _i64, _int, _vp, _vp, ctypes.POINTER(QueryOpts), _vp, _sz, _vp]),
+    "tk_batch_create": (_int, [ctypes.POINTER(_vp), _int, ctypes.POINTER(_i64), ctypes.POINTER(_i32),
+                                ctypes.POINTER(_vp)]),
+    "tk_batch_destroy": (_int, [_vp]),
+    "tk_batch_workspace_size": (_sz, [_vp]),
+    "tk_batch_output_size": (_i64, [_vp]),
+    "tk_batch_query": (_int, [_vp, _vp, _vp, _vp, _int, _vp, _sz, _vp]),
+    "tk_nn_distance_workspace_size": (_sz, [_i64, _i64, _int, _int, _int, _int]),
+    "tk_nn_distance": (_int, [_vp, _i64, _vp, _i64, _int, _int, _int, _int, _vp, _vp, _vp, _sz, _vp]),
     "tk_knn_backward_workspace_size": (_sz, [_i64, _int, _i64]),
     "tk_knn_backward": (_int, [_vp, _vp, _vp, _vp, _i64, _i64, _int, _int, _int, _vp, _vp, _vp, _sz, _vp]),
 }

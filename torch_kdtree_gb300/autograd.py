@@ -56,3 +56,27 @@ class KnnDistances(torch.autograd.Function):
             return None, None, None, None
         gq, gr = knn_backward(q, ref, idx, grad_dists, need_q, need_ref)
         return gq, gr, None, None
+
+
+class BruteDistances(torch.autograd.Function):
+    """dists, inds = BruteDistances.apply(q, ref, k, mode): exhaustive search
+    forward, same deterministic backward as the tree query."""
+
+    @staticmethod
+    def forward(ctx, q, ref, k, mode):
+        from .nn_distance import nn_distance_raw
+        d = torch.empty((q.shape[0], k), dtype=q.dtype, device=q.device)
+        i = torch.empty((q.shape[0], k), dtype=torch.int32, device=q.device)
+        nn_distance_raw(ref.detach(), q.detach(), k, d, i, mode)
+        ctx.save_for_backward(q, ref, i)
+        ctx.mark_non_differentiable(i)
+        return d, i
+
+    @staticmethod
+    def backward(ctx, grad_dists, _grad_idx):
+        q, ref, idx = ctx.saved_tensors
+        need_q, need_ref = ctx.needs_input_grad[0], ctx.needs_input_grad[1]
+        if not (need_q or need_ref):
+            return None, None, None, None
+        gq, gr = knn_backward(q, ref, idx, grad_dists, need_q, need_ref)
+        return gq, gr, None, None

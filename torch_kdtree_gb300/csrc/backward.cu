@@ -23,15 +23,16 @@ namespace {
 
 size_t align256(size_t v) { return (v + 255) / 256 * 256; }
 
+// D: compile-time upper bound of the runtime dimension d (d <= D).
 template <typename T, int D>
 __global__ void k_grad_q(const T* __restrict__ q, const T* __restrict__ ref, const int32_t* __restrict__ idx,
-                         const T* __restrict__ g, int nq, int n, int k, T* __restrict__ grad_q) {
+                         const T* __restrict__ g, int nq, int n, int k, int d, T* __restrict__ grad_q) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nq) return;
     T qi[D], acc[D];
 #pragma unroll
     for (int c = 0; c < D; ++c) {
-        qi[c] = q[(long long)i * D + c];
+        qi[c] = c < d ? q[(long long)i * d + c] : T(0);
         acc[c] = T(0);
     }
     for (int j = 0; j < k; ++j) {
@@ -39,10 +40,12 @@ __global__ void k_grad_q(const T* __restrict__ q, const T* __restrict__ ref, con
         if (m < 0 || m >= n) continue;
         const T w = T(2) * g[(long long)i * k + j];
 #pragma unroll
-        for (int c = 0; c < D; ++c) acc[c] += w * (qi[c] - ref[(long long)m * D + c]);
+        for (int c = 0; c < D; ++c)
+            if (c < d) acc[c] += w * (qi[c] - ref[(long long)m * d + c]);
     }
 #pragma unroll
-    for (int c = 0; c < D; ++c) grad_q[(long long)i * D + c] = acc[c];
+    for (int c = 0; c < D; ++c)
+        if (c < d) grad_q[(long long)i * d + c] = acc[c];
 }
 
 // keys: neighbour index (n for invalid entries, which sort last).
@@ -71,13 +74,13 @@ __global__ void k_segment_bounds(const uint32_t* __restrict__ keys, long long np
 template <typename T, int D>
 __global__ void k_grad_ref(const T* __restrict__ q, const T* __restrict__ ref, const T* __restrict__ g,
                            const uint32_t* __restrict__ pairs, const int* __restrict__ seg_start,
-                           const int* __restrict__ seg_end, int n, int k, T* __restrict__ grad_ref) {
+                           const int* __restrict__ seg_end, int n, int k, int d, T* __restrict__ grad_ref) {
     const int m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= n) return;
     T rm[D], acc[D];
 #pragma unroll
     for (int c = 0; c < D; ++c) {
-        rm[c] = ref[(long long)m * D + c];
+        rm[c] = c < d ? ref[(long long)m * d + c] : T(0);
         acc[c] = T(0);
     }
     const int end = seg_end[m];
@@ -87,10 +90,12 @@ __global__ void k_grad_ref(const T* __restrict__ q, const T* __restrict__ ref, c
         const long long i = (long long)(p / uint32_t(k));
         const T w = T(2) * g[p];
 #pragma unroll
-        for (int c = 0; c < D; ++c) acc[c] += w * (rm[c] - q[i * D + c]);
+        for (int c = 0; c < D; ++c)
+            if (c < d) acc[c] += w * (rm[c] - q[i * d + c]);
     }
 #pragma unroll
-    for (int c = 0; c < D; ++c) grad_ref[(long long)m * D + c] = acc[c];
+    for (int c = 0; c < D; ++c)
+        if (c < d) grad_ref[(long long)m * d + c] = acc[c];
 }
 
 struct BwLayout {
@@ -124,9 +129,10 @@ int key_bits_for(int64_t n) {
 }
 
 template <typename T, int D>
-int run_backward(const T* q, const T* ref, const int32_t* idx, const T* g, int nq, int n, int k, T* grad_q,
+int run_backward(const T* q, const T* ref, const int32_t* idx, const T* g, int nq, int n, int k, int d, T* grad_q,
                  T* grad_ref, char* ws, cudaStream_t s) {
-    if (grad_q) k_grad_q<T, D><<<(nq + 255) / 256, 256, 0, s>>>(q, ref, idx, g, nq, n, k, grad_q);
+    const int bs = D > 32 ? 64 : 256;
+    if (grad_q) k_grad_q<T, D><<<(nq + bs - 1) / bs, bs, 0, s>>>(q, ref, idx, g, nq, n, k, d, grad_q);
     if (grad_ref) {
         const BwLayout w = bw_layout(nq, k, n);
         const long long np = (long long)nq * k;
@@ -144,7 +150,7 @@ int run_backward(const T* q, const T* ref, const int32_t* idx, const T* g, int n
         cudaError_t e = cudaMemsetAsync(seg_end, 0, sizeof(int) * size_t(n), s);
         if (e != cudaSuccess) return fail(TK_ECUDA, std::string("memset: ") + cudaGetErrorString(e));
         if (np > 0) k_segment_bounds<<<unsigned((np + 255) / 256), 256, 0, s>>>(sk, np, n, seg_start, seg_end);
-        k_grad_ref<T, D><<<(n + 255) / 256, 256, 0, s>>>(q, ref, g, sv, seg_start, seg_end, n, k, grad_ref);
+        k_grad_ref<T, D><<<(n + bs - 1) / bs, bs, 0, s>>>(q, ref, g, sv, seg_start, seg_end, n, k, d, grad_ref);
     }
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return fail(TK_ECUDA, std::string("backward launch: ") + cudaGetErrorString(e));
@@ -170,7 +176,7 @@ int tk_knn_backward(const void* q, const void* ref, const int32_t* idx, const vo
     if (nq < 0 || nq >= (int64_t(1) << 31) || n < 1 || n >= (int64_t(1) << 31) || k < 1)
         return fail(TK_EINVAL, "bad sizes");
     if (nq * int64_t(k) >= (int64_t(1) << 31)) return fail(TK_EINVAL, "nq * k must be < 2^31");
-    if (dims < 1 || dims > 3) return fail(TK_EINVAL, "dims must be 1, 2 or 3");
+    if (dims < 1 || dims > 128) return fail(TK_EINVAL, "dims must be in [1, 128]");
     if (dtype != TK_F32 && dtype != TK_F64) return fail(TK_EINVAL, "dtype must be TK_F32 or TK_F64");
     if (nq == 0 && !grad_ref) return TK_OK;
     if (!q || !ref || !idx || !grad_dists) return fail(TK_EINVAL, "null input pointer");
@@ -179,19 +185,25 @@ int tk_knn_backward(const void* q, const void* ref, const int32_t* idx, const vo
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     char* ws = static_cast<char*>(workspace);
     const int nq32 = int(nq), n32 = int(n);
-#define TK_BW(TT, DD)                                                                                       \
-    return run_backward<TT, DD>(static_cast<const TT*>(q), static_cast<const TT*>(ref), idx,                \
-                                static_cast<const TT*>(grad_dists), nq32, n32, k, static_cast<TT*>(grad_q), \
-                                static_cast<TT*>(grad_ref), ws, s)
+#define TK_BW(TT, DD)                                                                                        \
+    return run_backward<TT, DD>(static_cast<const TT*>(q), static_cast<const TT*>(ref), idx,                 \
+                                static_cast<const TT*>(grad_dists), nq32, n32, k, dims,                      \
+                                static_cast<TT*>(grad_q), static_cast<TT*>(grad_ref), ws, s)
+#define TK_BW_ALL(TT)                   \
+    if (dims == 1) TK_BW(TT, 1);        \
+    if (dims == 2) TK_BW(TT, 2);        \
+    if (dims == 3) TK_BW(TT, 3);        \
+    if (dims <= 8) TK_BW(TT, 8);        \
+    if (dims <= 16) TK_BW(TT, 16);      \
+    if (dims <= 32) TK_BW(TT, 32);      \
+    if (dims <= 64) TK_BW(TT, 64);      \
+    TK_BW(TT, 128);
     if (dtype == TK_F32) {
-        if (dims == 1) TK_BW(float, 1);
-        if (dims == 2) TK_BW(float, 2);
-        TK_BW(float, 3);
+        TK_BW_ALL(float)
     } else {
-        if (dims == 1) TK_BW(double, 1);
-        if (dims == 2) TK_BW(double, 2);
-        TK_BW(double, 3);
+        TK_BW_ALL(double)
     }
+#undef TK_BW_ALL
 #undef TK_BW
 }
 

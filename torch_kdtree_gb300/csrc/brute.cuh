@@ -1,0 +1,127 @@
+// Exhaustive ("brute force") exact KNN: the nn_distance op.
+//
+// The reference's kernel (NmDistanceKernelDynamic, src/nndistance_g.cu:74-140)
+// runs as ONE block for the whole problem, hard-codes d = 3 and keeps each
+// thread's top-k list in a global scratch array.  Here:
+//   * a block owns a tile of queries (one query per group of G lanes) and one
+//     slice of the reference cloud; the grid is queries x slices so every SM
+//     is busy even for few queries;
+//   * reference points stream through shared memory in tiles, zero-padded to
+//     DP dimensions (padding adds exact zeros, so distances are unchanged);
+//   * distances use the reference's CPU arithmetic (sqdist order, no fused
+//     multiply-add), so results match the KD-tree query bit for bit;
+//   * each slice keeps the k best (distance, index) keys in registers (TopK);
+//     with several slices a merge kernel combines the per-slice lists.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "tk_device.cuh"
+#include "tk_internal.h"
+
+namespace tk {
+
+template <typename T>
+struct BruteArgs {
+    const T* ref;   // [n, d]
+    const T* q;     // [nq, d]
+    int n, nq, d, k;
+    int nsplit;     // reference slices (gridDim.y)
+    T* out_d;       // [nq, k]   (nsplit == 1)
+    int32_t* out_i; // [nq, k]
+    Key<T>* part;   // [nq, nsplit, k] per-slice lists (nsplit > 1)
+};
+
+template <int DP>
+struct BruteTile {
+    static constexpr int kRefs = (8192 / DP) > 256 ? 256 : ((8192 / DP) < 32 ? 32 : (8192 / DP));
+};
+
+template <typename T, int DP>
+__device__ __forceinline__ T sqdist_padded(const T (&q)[DP], const T* r) {
+    T d0 = sub_rn(q[0], r[0]);
+    T acc = mul_rn(d0, d0);
+#pragma unroll
+    for (int c = 1; c < DP; ++c) {
+        const T dc = sub_rn(q[c], r[c]);
+        acc = add_rn(acc, mul_rn(dc, dc));
+    }
+    return acc;
+}
+
+template <typename T, int DP, int G, int R>
+__global__ void __launch_bounds__(256) k_brute(const BruteArgs<T> a) {
+    constexpr int TR = BruteTile<DP>::kRefs;
+    __shared__ __align__(16) T tile[TR * DP];
+    const int lane = threadIdx.x & 31;
+    const int gl = lane & (G - 1);
+    const int gbase = lane & ~(G - 1);
+    const unsigned gmask = group_mask<G>(lane);
+    const int qi = blockIdx.x * (blockDim.x / G) + threadIdx.x / G;
+    const bool active = qi < a.nq;
+
+    T q[DP];
+#pragma unroll
+    for (int c = 0; c < DP; ++c) q[c] = (active && c < a.d) ? a.q[(long long)qi * a.d + c] : T(0);
+
+    TopK<T, G, R> list;
+    list.init(a.k, gl);
+    Key<T> worst = Key<T>::sentinel();
+
+    const long long per = ((long long)a.n + a.nsplit - 1) / a.nsplit;
+    const int r0 = int(min((long long)a.n, per * blockIdx.y));
+    const int r1 = int(min((long long)a.n, per * (blockIdx.y + 1)));
+    for (int t0 = r0; t0 < r1; t0 += TR) {
+        const int len = min(TR, r1 - t0);
+        __syncthreads();
+        for (int e = threadIdx.x; e < TR * DP; e += blockDim.x) {
+            const int j = e / DP, c = e - j * DP;
+            tile[e] = (j < len && c < a.d) ? a.ref[(long long)(t0 + j) * a.d + c] : T(0);
+        }
+        __syncthreads();
+        if (active) {
+            for (int j0 = 0; j0 < len; j0 += G) {
+                const int j = j0 + gl;
+                Key<T> mine = Key<T>::sentinel();
+                if (j < len) mine = Key<T>::make(sqdist_padded<T, DP>(q, tile + j * DP), uint32_t(t0 + j));
+                worst = offer<T, G, R>(list, mine, worst, gmask, gl, gbase);
+            }
+        }
+    }
+    if (!active) return;
+    if (a.nsplit == 1) {
+        list.store(a.k, gl, a.out_d, a.out_i, qi);
+    } else {
+        Key<T>* dst = a.part + ((long long)qi * a.nsplit + blockIdx.y) * a.k;
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const int s = r * G + gl;
+            const int o = s - (G * R - a.k);
+            if (o >= 0) dst[o] = list.slot[r];
+        }
+    }
+}
+
+// Combine the per-slice lists of every query (group of G lanes per query).
+template <typename T, int G, int R>
+__global__ void __launch_bounds__(256) k_brute_merge(const BruteArgs<T> a) {
+    const int lane = threadIdx.x & 31;
+    const int gl = lane & (G - 1);
+    const int gbase = lane & ~(G - 1);
+    const unsigned gmask = group_mask<G>(lane);
+    const int qi = blockIdx.x * (blockDim.x / G) + threadIdx.x / G;
+    if (qi >= a.nq) return;  // whole groups leave together
+    TopK<T, G, R> list;
+    list.init(a.k, gl);
+    Key<T> worst = Key<T>::sentinel();
+    const Key<T>* src = a.part + (long long)qi * a.nsplit * a.k;
+    const int total = a.nsplit * a.k;
+    for (int e0 = 0; e0 < total; e0 += G) {
+        const int e = e0 + gl;
+        const Key<T> mine = e < total ? src[e] : Key<T>::sentinel();
+        worst = offer<T, G, R>(list, mine, worst, gmask, gl, gbase);
+    }
+    list.store(a.k, gl, a.out_d, a.out_i, qi);
+}
+
+}  // namespace tk

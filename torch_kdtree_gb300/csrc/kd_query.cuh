@@ -71,16 +71,24 @@ __device__ __forceinline__ T pick(const T (&v)[D], int ax) {
     return r;
 }
 
-// Exhaustive-equivalent KNN for one query, served by a group of G lanes.
-template <typename T, int D, int G, int R>
-__device__ __forceinline__ void kd_query_one(const KdArgs<T>& a, const T* s_med, int qi, unsigned gmask,
-                                             int gl, int gbase) {
-    T q[D];
-#pragma unroll
-    for (int c = 0; c < D; ++c) q[c] = a.q[(long long)qi * D + c];
+// One tree as the search sees it.
+template <typename T>
+struct TreeView {
+    const PointRec<T>* pts;
+    const T* medians;
+    const int32_t* leaf_off;
+    int levels;
+    int smem_levels;  // top levels whose split values are in s_med
+    const T* s_med;
+};
 
+// Exhaustive-equivalent KNN for one query, served by a group of G lanes;
+// writes k results to out_d[0..k) / out_i[0..k).
+template <typename T, int D, int G, int R>
+__device__ __forceinline__ void kd_search(const TreeView<T>& tv, const T (&q)[D], int k, T* out_d,
+                                          int32_t* out_i, unsigned gmask, int gl, int gbase) {
     TopK<T, G, R> list;
-    list.init(a.k, gl);
+    list.init(k, gl);
     Key<T> worst = Key<T>::sentinel();
     T worst_d = worst.dist();
 
@@ -90,14 +98,14 @@ __device__ __forceinline__ void kd_query_one(const KdArgs<T>& a, const T* s_med,
     T e[D];
 #pragma unroll
     for (int c = 0; c < D; ++c) e[c] = T(0);
-    const int L = a.levels;
+    const int L = tv.levels;
     const int first_leaf = (1 << L) - 1;
 
     for (;;) {
         // descend to the near leaf, stacking far siblings that may matter
         int ax = depth % D;
         while (depth < L) {
-            const T m = depth < a.smem_levels ? s_med[node] : __ldg(a.medians + node);
+            const T m = depth < tv.smem_levels ? tv.s_med[node] : __ldg(tv.medians + node);
             const T qa = pick<T, D>(q, ax);
             const T diff = sub_rn(qa, m);
             const T plane = mul_rn(diff, diff);
@@ -114,13 +122,13 @@ __device__ __forceinline__ void kd_query_one(const KdArgs<T>& a, const T* s_med,
         // scan the leaf bucket, G points at a time
         {
             const int leaf = node - first_leaf;
-            const int beg = __ldg(a.leaf_off + leaf);
-            const int end = __ldg(a.leaf_off + leaf + 1);
+            const int beg = __ldg(tv.leaf_off + leaf);
+            const int end = __ldg(tv.leaf_off + leaf + 1);
             for (int j0 = beg; j0 < end; j0 += G) {
                 const int j = j0 + gl;
                 Key<T> mine = Key<T>::sentinel();
                 if (j < end) {
-                    const PointRec<T> p = load_rec(a.pts + j);
+                    const PointRec<T> p = load_rec(tv.pts + j);
                     mine = Key<T>::make(sqdist<T, D>(q, p), rec_index(p));
                 }
                 worst = offer<T, G, R>(list, mine, worst, gmask, gl, gbase);
@@ -142,7 +150,18 @@ __device__ __forceinline__ void kd_query_one(const KdArgs<T>& a, const T* s_med,
         }
         if (!resumed) break;
     }
-    list.store(a.k, gl, a.out_d, a.out_i, qi);
+    list.store(k, gl, out_d, out_i, 0);
+}
+
+template <typename T, int D, int G, int R>
+__device__ __forceinline__ void kd_query_one(const KdArgs<T>& a, const T* s_med, int qi, unsigned gmask, int gl,
+                                             int gbase) {
+    T q[D];
+#pragma unroll
+    for (int c = 0; c < D; ++c) q[c] = a.q[(long long)qi * D + c];
+    const TreeView<T> tv{a.pts, a.medians, a.leaf_off, a.levels, a.smem_levels, s_med};
+    kd_search<T, D, G, R>(tv, q, a.k, a.out_d + (long long)qi * a.k, a.out_i + (long long)qi * a.k, gmask, gl,
+                          gbase);
 }
 
 template <typename T, int D, int G, int R>

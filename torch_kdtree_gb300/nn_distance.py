@@ -207,3 +207,56 @@ def build_kd_tree(points_ref: Union[torch.Tensor, np.ndarray], device: Optional[
     assert device.type != "cuda" or gpu_available, "You requested the KD-Tree on the GPU, but no CUDA device is visible"
     assert device.type in ["cuda", "cpu"]
     return TorchKDTree(points_ref, device, levels, squared_distances, query_opts)
+
+
+_BRUTE_MODES = {"exact": _lib.TK_BRUTE_EXACT, "fp32": _lib.TK_BRUTE_EXACT, "fp64": _lib.TK_BRUTE_EXACT,
+                "tf32": _lib.TK_BRUTE_TF32, "bf16_split": _lib.TK_BRUTE_BF16_SPLIT}
+
+
+def nn_distance_raw(points_ref: torch.Tensor, points_query: torch.Tensor, k: int, dists: torch.Tensor,
+                    idx: torch.Tensor, mode: str = "exact") -> None:
+    """Enqueue one tk_nn_distance on the current stream (inputs on the device)."""
+    m = _BRUTE_MODES[mode]
+    n, d = points_ref.shape
+    nq = points_query.shape[0]
+    dt = _DTYPES[points_ref.dtype]
+    ws_bytes = LIB.tk_nn_distance_workspace_size(n, nq, d, k, dt, m)
+    ws = _workspace(ws_bytes, points_ref.device)
+    check(LIB.tk_nn_distance(points_ref.data_ptr(), n, points_query.data_ptr(), nq, d, k, dt, m,
+                             dists.data_ptr(), idx.data_ptr(), ws.data_ptr(), ws_bytes,
+                             _stream_ptr(points_ref.device)))
+
+
+def nn_distance(points_ref: torch.Tensor, points_query: torch.Tensor, nr_nns_searches: int = 1,
+                mode: str = "exact"):
+    """Exhaustive exact KNN: ``(dists, inds)`` of every query among all
+    reference points, squared distances ``[Q, k]`` and int32 indices.
+
+    ``mode``: "exact" (CUDA cores, float32 or float64), "tf32" or
+    "bf16_split" (tensor-core candidate search with an exact float32 re-rank;
+    same answer).  Differentiable in both point sets.  The reference shipped
+    this search as an unbound CUDA launcher (src/nndistance_g.cu:191-220) for
+    d = 3 only; here any 1 <= d <= 128 (float64: d <= 4)."""
+    if mode not in _BRUTE_MODES:
+        raise ValueError(f"mode must be one of {sorted(_BRUTE_MODES)}")
+    if points_ref.device.type != "cuda":
+        raise RuntimeError("nn_distance runs on CUDA tensors only")
+    if points_ref.dtype not in _DTYPES or points_query.dtype != points_ref.dtype:
+        raise AssertionError("points must be float32 or float64 and of the same dtype")
+    if points_ref.dim() != 2 or points_query.dim() != 2 or points_query.shape[1] != points_ref.shape[1]:
+        raise AssertionError("points must be [N, d] and [Q, d]")
+    k = int(nr_nns_searches)
+    if k > points_ref.shape[0]:
+        raise RuntimeError("You requested more nearest neighbors than there are reference points")
+    points_query = points_query.to(points_ref.device)
+    ref_c = points_ref.contiguous()
+    q_c = points_query.contiguous()
+    need_grad = torch.is_grad_enabled() and (points_ref.requires_grad or points_query.requires_grad)
+    if need_grad:
+        from .autograd import BruteDistances
+        return BruteDistances.apply(q_c, ref_c, k, mode)
+    nq = q_c.shape[0]
+    dists = torch.empty((nq, k), dtype=ref_c.dtype, device=ref_c.device)
+    idx = torch.empty((nq, k), dtype=torch.int32, device=ref_c.device)
+    nn_distance_raw(ref_c.detach(), q_c.detach(), k, dists, idx, mode)
+    return dists, idx
