@@ -110,6 +110,25 @@ size_t tk_tree_query_workspace_size(const tk_tree* tree, int64_t nq);
 int tk_tree_query(const tk_tree* tree, const void* q, int64_t nq, int k, void* dists, int32_t* idx,
                   const tk_query_opts* opts, void* workspace, size_t workspace_bytes, void* stream);
 
+/* Largest query count tk_tree_query_noalloc accepts in one call. */
+#define TK_NOALLOC_MAX_QUERIES 262144
+
+/* tk_tree_query without a caller workspace and without any allocation.
+ * No counterpart in the reference: it exists for callers that cannot call
+ * cudaMalloc on their query path -- hosts whose device memory belongs to
+ * another allocator, plain C/FFI callers with no device allocator of their
+ * own, and latency-critical code where cudaMalloc (which synchronises the
+ * device) is not acceptable.  Scratch comes from a static device array of
+ * about 3.3 MiB built into the library (held on every GPU that loads it until
+ * the process exits).  At most TK_NOALLOC_MAX_QUERIES queries per call; more
+ * fails with TK_EINVAL.  Every call on a device shares that array: calls that
+ * may overlap on the GPU (different streams, or threads without ordering)
+ * race and must be serialised by the caller.  The first call on a device
+ * looks up the array's device address; make that first call before any
+ * stream capture.  Results are identical to tk_tree_query's. */
+int tk_tree_query_noalloc(const tk_tree* tree, const void* q, int64_t nq, int k, void* dists, int32_t* idx,
+                          const tk_query_opts* opts, void* stream);
+
 /* ------------------------------------------------------------ batches -- */
 
 typedef struct tk_batch tk_batch;

@@ -23,6 +23,7 @@ TK_F64 = 1
 TK_BRUTE_EXACT = 0
 TK_BRUTE_TF32 = 1
 TK_BRUTE_BF16_SPLIT = 2
+TK_NOALLOC_MAX_QUERIES = 262144
 
 _STATUS_NAMES = {
     TK_EINVAL: "EINVAL", TK_ENOMEM: "ENOMEM", TK_EUNSUPPORTED: "EUNSUPPORTED",
@@ -84,6 +85,7 @@ SIGNATURES = {
     "tk_batch_query": (_int, [_vp, _vp, _vp, _vp, _int, _vp, _sz, _vp]),
     "tk_nn_distance_workspace_size": (_sz, [_i64, _i64, _int, _int, _int, _int]),
     "tk_nn_distance": (_int, [_vp, _i64, _vp, _i64, _int, _int, _int, _int, _vp, _vp, _vp, _sz, _vp]),
+    "tk_tree_query_noalloc": (_int, [_vp, _vp, _i64, _int, _vp, _vp, ctypes.POINTER(QueryOpts), _vp]),
     "tk_knn_backward_workspace_size": (_sz, [_i64, _int, _i64]),
     "tk_knn_backward": (_int, [_vp, _vp, _vp, _vp, _i64, _i64, _int, _int, _int, _vp, _vp, _vp, _sz, _vp]),
 }

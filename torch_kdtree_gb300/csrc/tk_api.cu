@@ -436,3 +436,84 @@ int tk_tree_query(const tk_tree* t, const void* q, int64_t nq, int k, void* dist
 }
 
 }  // extern "C"
+
+// ------------------------------------------------ allocation-free query --
+//
+// Scratch of tk_tree_query_noalloc: one static device array, sized for
+// TK_NOALLOC_MAX_QUERIES queries (counter + 2^16 cell counts + three int32
+// arrays of that many queries, laid out as ws_layout() lays out a caller's
+// workspace).  Every GPU that loads the library holds it until the process
+// exits, and every call on a device shares it.
+namespace tk {
+namespace {
+
+constexpr size_t kNoAllocScratchBytes =
+    256 + sizeof(int) * (size_t(1) << kMaxBinLevels) + 3 * sizeof(int) * size_t(TK_NOALLOC_MAX_QUERIES);
+static_assert(TK_NOALLOC_MAX_QUERIES % 64 == 0, "each scratch array must stay 256-byte aligned");
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+void* g_noalloc_ptr[kNoAllocMaxDevices] = {};
+
+// Device address of g_noalloc_scratch on the current device (looked up once
+// per device; in host code the symbol itself is only a host-side stand-in).
+int noalloc_scratch(int dev, void** out) {
+    if (dev < 0 || dev >= kNoAllocMaxDevices) return fail(TK_EINVAL, "device ordinal out of range");
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p)
+            return fail(TK_ECUDA, std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
+        g_noalloc_ptr[dev] = p;
+    }
+    *out = g_noalloc_ptr[dev];
+    return TK_OK;
+}
+
+}  // namespace
+}  // namespace tk
+
+extern "C" int tk_tree_query_noalloc(const tk_tree* t, const void* q, int64_t nq, int k, void* dists, int32_t* idx,
+                                     const tk_query_opts* opts, void* stream) {
+    clear_error();
+    if (!t) return fail(TK_EINVAL, "tree is null");
+    if (nq < 0 || nq > TK_NOALLOC_MAX_QUERIES)
+        return fail(TK_EINVAL, "tk_tree_query_noalloc takes at most " + std::to_string(TK_NOALLOC_MAX_QUERIES) +
+                                   " queries per call (got " + std::to_string(nq) + "); split the batch");
+    if (k < 1) return fail(TK_EINVAL, "k must be >= 1");
+    if (k > t->n) return fail(TK_EINVAL, "You requested more nearest neighbors than there are in the KD-Tree");
+    if (k > kMaxK) return fail(TK_EINVAL, "k is limited to 128 on the GPU");
+    if (t->device < 0 || !t->d_pts) return fail(TK_EINVAL, "tree was built host-only (device < 0); it has no device image");
+    if (nq == 0) return TK_OK;
+    if (!q || !dists || !idx) return fail(TK_EINVAL, "null query or output pointer");
+    DeviceGuard g(t->device);
+    void* scratch = nullptr;
+    int rc = noalloc_scratch(t->device, &scratch);
+    if (rc != TK_OK) return rc;
+    if (ws_layout(t->levels, nq).total > kNoAllocScratchBytes)
+        return fail(TK_EINVAL, "query needs more scratch than the static array holds");
+    tk_query_opts o{0, -1, -1, 0, 0, nullptr, nullptr};
+    if (opts) o = *opts;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    char* ws = static_cast<char*>(scratch);
+    const int n32 = int(nq);
+    if (t->dtype == TK_F32) {
+        auto* qq = static_cast<const float*>(q);
+        auto* dd = static_cast<float*>(dists);
+        switch (t->dims) {
+            case 1: return run_query<float, 1>(t, qq, n32, k, dd, idx, o, ws, s);
+            case 2: return run_query<float, 2>(t, qq, n32, k, dd, idx, o, ws, s);
+            default: return run_query<float, 3>(t, qq, n32, k, dd, idx, o, ws, s);
+        }
+    }
+    auto* qq = static_cast<const double*>(q);
+    auto* dd = static_cast<double*>(dists);
+    switch (t->dims) {
+        case 1: return run_query<double, 1>(t, qq, n32, k, dd, idx, o, ws, s);
+        case 2: return run_query<double, 2>(t, qq, n32, k, dd, idx, o, ws, s);
+        default: return run_query<double, 3>(t, qq, n32, k, dd, idx, o, ws, s);
+    }
+}
