@@ -529,6 +529,53 @@ def run_brute(args):
 
 
 
+def run_brute_tc(args):
+    """Tensor-core brute force vs the FP32 CUDA-core brute force: 262,144 refs,
+    65,536 queries, N(0,1) in d = 8 and 32 with 5% exact duplicate refs, k=32.
+    The tensor-core modes over-fetch 2k candidates, re-rank them exactly and
+    recompute uncertified queries exactly; all modes must agree bit for bit."""
+    import torch
+
+    from torch_kdtree_gb300.nn_distance import nn_distance_raw
+    from torch_kdtree_gb300.synthetic import tensor_core_brute
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    k = 32
+    out = {}
+    for d in (8, 32):
+        ref_np, q_np = tensor_core_brute(d=d)
+        ref = torch.from_numpy(ref_np).to(dev)
+        q = torch.from_numpy(q_np).to(dev)
+        res = {}
+        base = None
+        for mode in ("exact", "tf32", "bf16_split"):
+            dd = torch.empty(len(q), k, device=dev)
+            ii = torch.empty(len(q), k, dtype=torch.int32, device=dev)
+            ms = _event_ms(lambda: nn_distance_raw(ref, q, k, dd, ii, mode), args.steps, args.warmup)
+            t = sum(ms) / len(ms) / 1e3
+            pairs = len(ref) * len(q)
+            r = {"ms": 1e3 * t, "pairs_per_s": pairs / t, "tflops_2d": 2 * d * pairs / t / 1e12}
+            if base is None:
+                base = (dd.clone(), ii.clone())
+            else:
+                r["rows_with_index_mismatch_vs_exact"] = int((ii != base[1]).any(1).sum().item())
+                r["dist_bit_mismatch_vs_exact"] = int((dd.view(torch.int32) != base[0].view(torch.int32)).sum().item())
+                r["speedup_vs_exact"] = res["exact"]["ms"] / r["ms"]
+            res[mode] = r
+        out[f"d{d}"] = res
+    best = min(out["d32"]["tf32"]["ms"], out["d32"]["bf16_split"]["ms"])
+    line = {
+        "metric": "tensor-core brute-force speed-up over FP32 brute force at d=32 (262,144 x 65,536, k=32, exact)",
+        "value": out["d32"]["exact"]["ms"] / best, "unit": "x", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": best, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 inputs (tf32 / bf16 hi-lo products, fp32 re-rank)",
+        "data": "synthetic (seeded numpy N(0,1), 5% duplicate refs)",
+        "config": {"workload": "262,144 refs x 65,536 queries, d in {8, 32}, k=32, over-fetch 2k"},
+        "runs": out,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
@@ -540,7 +587,7 @@ def main():
     p.add_argument("--levels", type=int, default=0, help="chosen tree depth (skips the autotuner with --tpq)")
     p.add_argument("--tpq", type=int, default=0, help="chosen lanes per query (skips the autotuner with --levels)")
     p.add_argument("--profile", action="store_true", help="run one chosen and one plain query only (for ncu)")
-    p.add_argument("--workload", default="kd", choices=["kd", "batched", "backward", "brute"],
+    p.add_argument("--workload", default="kd", choices=["kd", "batched", "backward", "brute", "brute_tc"],
                    help="kd (default): the headline large single-cloud query; the others measure the "
                         "batched, backward and brute-force paths")
     p.add_argument("--leaf-size", type=int, default=16, help="target points per leaf of tuned batch trees")
@@ -554,7 +601,8 @@ def main():
         return
     if args.workload != "kd":
         if rank == 0:
-            {"batched": run_batched, "backward": run_backward, "brute": run_brute}[args.workload](args)
+            {"batched": run_batched, "backward": run_backward, "brute": run_brute,
+             "brute_tc": run_brute_tc}[args.workload](args)
         return
     if world > 1:
         import torch

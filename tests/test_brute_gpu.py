@@ -88,3 +88,36 @@ def test_errors():
         tk().nn_distance(ref, torch.randn(4, 2, device=cuda), 1)
     with pytest.raises(Exception):
         tk().nn_distance(ref, torch.randn(4, 3, device=cuda, dtype=torch.float64), 1)
+
+
+@pytest.mark.parametrize("mode", ["tf32", "bf16_split"])
+@pytest.mark.parametrize("d", [3, 8, 17, 32, 64])
+@pytest.mark.parametrize("k", [1, 16, 32])
+def test_tensor_core_modes_are_exact(mode, d, k, oracle):
+    """Tensor-core candidate search + exact re-rank (+ exact fallback for
+    uncertified queries) returns the exact answer, bit for bit."""
+    rng = np.random.default_rng(1000 + 10 * d + k)
+    ref = rng.standard_normal((20000, d)).astype(np.float32)
+    m = 1000
+    perm = rng.permutation(len(ref))
+    ref[perm[:m]] = ref[perm[m:2 * m]]  # 5% exact duplicates
+    q = rng.standard_normal((3000, d)).astype(np.float32)
+    dd, ii = tk().nn_distance(torch.from_numpy(ref).to(cuda), torch.from_numpy(q).to(cuda), k, mode=mode)
+    bd, bi = oracle.brute(ref, q, k)
+    np.testing.assert_array_equal(dd.cpu().numpy(), bd)
+    np.testing.assert_array_equal(ii.cpu().numpy(), bi)
+
+
+@pytest.mark.parametrize("mode", ["tf32", "bf16_split"])
+def test_tensor_core_fallback_on_massive_ties(mode, oracle):
+    """64 distinct points repeated ~300 times: candidate lists cannot separate
+    the k-th neighbour from the rest, the certificate fails and the exact
+    fallback must produce the answer."""
+    rng = np.random.default_rng(7)
+    base = rng.standard_normal((64, 16)).astype(np.float32)
+    ref = base[rng.integers(0, 64, 20000)]
+    q = rng.standard_normal((500, 16)).astype(np.float32)
+    dd, ii = tk().nn_distance(torch.from_numpy(ref).to(cuda), torch.from_numpy(q).to(cuda), 20, mode=mode)
+    bd, bi = oracle.brute(ref, q, 20)
+    np.testing.assert_array_equal(dd.cpu().numpy(), bd)
+    np.testing.assert_array_equal(ii.cpu().numpy(), bi)

@@ -138,6 +138,48 @@ int check_common(const void* ref, int64_t n, const void* q, int64_t nq, int d, i
 }
 
 }  // namespace
+
+// The fallback expects few listed queries: it slices the references finely
+// (as planned for 1,024 queries) and launches for the worst case of all nq;
+// blocks past the device-side count exit at once.
+size_t brute_fallback_workspace_bytes(int64_t n, int64_t nq, int d, int k) {
+    BrutePlan p = plan_brute(n, std::min<int64_t>(std::max<int64_t>(nq, 1), 1024), d, k);
+    if (p.nsplit <= 1) return 256;
+    return align256(sizeof(Key<float>) * size_t(std::max<int64_t>(nq, 1)) * p.nsplit * k);
+}
+
+int brute_fallback(const float* ref, int64_t n, const float* q, int64_t nq, int d, int k, float* dists,
+                   int32_t* idx, const int* qlist, const int* qcount, void* ws, size_t ws_bytes, cudaStream_t s) {
+    BrutePlan p = plan_brute(n, std::min<int64_t>(std::max<int64_t>(nq, 1), 1024), d, k);
+    const int per_block = 256 / p.G;
+    p.qtiles = int((nq + per_block - 1) / per_block);
+    if (ws_bytes < brute_fallback_workspace_bytes(n, nq, d, k)) return fail(TK_EWORKSPACE, "fallback workspace");
+    BruteArgs<float> a;
+    a.ref = ref;
+    a.q = q;
+    a.n = int(n);
+    a.nq = int(nq);
+    a.d = d;
+    a.k = k;
+    a.nsplit = p.nsplit;
+    a.out_d = dists;
+    a.out_i = idx;
+    a.part = static_cast<Key<float>*>(ws);
+    a.qlist = qlist;
+    a.qcount = qcount;
+    switch (p.DP) {
+        case 1: return launch_dp<float, 1>(a, p, s);
+        case 2: return launch_dp<float, 2>(a, p, s);
+        case 3: return launch_dp<float, 3>(a, p, s);
+        case 4: return launch_dp<float, 4>(a, p, s);
+        case 8: return launch_dp<float, 8>(a, p, s);
+        case 16: return launch_dp<float, 16>(a, p, s);
+        case 32: return launch_dp<float, 32>(a, p, s);
+        case 64: return launch_dp<float, 64>(a, p, s);
+        default: return launch_dp<float, 128>(a, p, s);
+    }
+}
+
 }  // namespace tk
 
 using namespace tk;

@@ -30,6 +30,10 @@ struct BruteArgs {
     T* out_d;       // [nq, k]   (nsplit == 1)
     int32_t* out_i; // [nq, k]
     Key<T>* part;   // [nq, nsplit, k] per-slice lists (nsplit > 1)
+    // Optional gather: when qlist is set, block slots index qlist[0..*qcount)
+    // and results go to rows qlist[slot]; slots past *qcount do nothing.
+    const int* qlist = nullptr;
+    const int* qcount = nullptr;
 };
 
 template <int DP>
@@ -57,8 +61,14 @@ __global__ void __launch_bounds__(256) k_brute(const BruteArgs<T> a) {
     const int gl = lane & (G - 1);
     const int gbase = lane & ~(G - 1);
     const unsigned gmask = group_mask<G>(lane);
-    const int qi = blockIdx.x * (blockDim.x / G) + threadIdx.x / G;
-    const bool active = qi < a.nq;
+    const int slot = blockIdx.x * (blockDim.x / G) + threadIdx.x / G;
+    int live = a.nq;
+    if (a.qlist) {
+        live = *a.qcount;
+        if (int(blockIdx.x * (blockDim.x / G)) >= live) return;  // whole block idle (uniform)
+    }
+    const bool active = slot < live;
+    const int qi = active ? (a.qlist ? a.qlist[slot] : slot) : 0;
 
     T q[DP];
 #pragma unroll
@@ -92,7 +102,7 @@ __global__ void __launch_bounds__(256) k_brute(const BruteArgs<T> a) {
     if (a.nsplit == 1) {
         list.store(a.k, gl, a.out_d, a.out_i, qi);
     } else {
-        Key<T>* dst = a.part + ((long long)qi * a.nsplit + blockIdx.y) * a.k;
+        Key<T>* dst = a.part + ((long long)slot * a.nsplit + blockIdx.y) * a.k;
 #pragma unroll
         for (int r = 0; r < R; ++r) {
             const int s = r * G + gl;
@@ -109,12 +119,14 @@ __global__ void __launch_bounds__(256) k_brute_merge(const BruteArgs<T> a) {
     const int gl = lane & (G - 1);
     const int gbase = lane & ~(G - 1);
     const unsigned gmask = group_mask<G>(lane);
-    const int qi = blockIdx.x * (blockDim.x / G) + threadIdx.x / G;
-    if (qi >= a.nq) return;  // whole groups leave together
+    const int slot = blockIdx.x * (blockDim.x / G) + threadIdx.x / G;
+    const int live = a.qlist ? *a.qcount : a.nq;
+    if (slot >= live) return;  // whole groups leave together
+    const int qi = a.qlist ? a.qlist[slot] : slot;
     TopK<T, G, R> list;
     list.init(a.k, gl);
     Key<T> worst = Key<T>::sentinel();
-    const Key<T>* src = a.part + (long long)qi * a.nsplit * a.k;
+    const Key<T>* src = a.part + (long long)slot * a.nsplit * a.k;
     const int total = a.nsplit * a.k;
     for (int e0 = 0; e0 < total; e0 += G) {
         const int e = e0 + gl;
@@ -123,5 +135,11 @@ __global__ void __launch_bounds__(256) k_brute_merge(const BruteArgs<T> a) {
     }
     list.store(a.k, gl, a.out_d, a.out_i, qi);
 }
+
+// Exact search for the queries listed on the device (qlist[0..*qcount)),
+// results written to their rows of dists / idx (brute.cu).
+size_t brute_fallback_workspace_bytes(int64_t n, int64_t nq, int d, int k);
+int brute_fallback(const float* ref, int64_t n, const float* q, int64_t nq, int d, int k, float* dists,
+                   int32_t* idx, const int* qlist, const int* qcount, void* ws, size_t ws_bytes, cudaStream_t s);
 
 }  // namespace tk
