@@ -27,6 +27,7 @@
 
 #include "brute.cuh"
 #include "brute_tc.cuh"
+#include "tc_sm100.cuh"
 #include "tk_internal.h"
 
 namespace tk {
@@ -242,6 +243,264 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc_select(const TcArgs a) {
     }
 }
 
+// ---------------------------------------------------------------------------
+// tcgen05 path (d <= 39 for TF32, d <= 47 for BF16 split; k <= 32).
+//
+// The score is produced by the MMA itself by augmenting K with one column:
+//   A = [-2 q, 1, 0...],  B = [r, |r|^2, 0...]  =>  A.B = |r|^2 - 2 q.r.
+// Operands are packed in global memory in the tensor core's canonical
+// no-swizzle K-major layout (8-row x 16-byte core matrices; core matrices
+// adjacent along K 128 bytes apart, 8-row groups 8*KB bytes apart), one
+// contiguous block per 128 query rows / 256 reference rows, so each tile is
+// a single bulk copy.  Reference padding rows carry a huge |r|^2 and never
+// become candidates.
+constexpr int kT5Rows = 128;   // M (queries per block)
+constexpr int kT5Cols = 256;   // N (references per tile)
+constexpr int kT5EpiWarps = 8; // two warps per 32-lane quarter of the accumulator, one column half each
+constexpr int kT5Threads = 32 * (kT5EpiWarps + 1);
+constexpr float kT5PadNorm = 1e30f;
+constexpr uint32_t kT5MaxTries = 1u << 22;  // bounded mbarrier polls
+
+__device__ __forceinline__ uint32_t core_offset(int row, int kb, int KB) {
+    return uint32_t((row >> 3) * (8 * KB) + (kb >> 4) * 128 + (row & 7) * 16 + (kb & 15));
+}
+
+// rows: logical rows; padded to a multiple of tile_rows.  is_query selects
+// [-2q, 1] (queries) or [r, |r|^2] (references).
+template <int MODE>
+__global__ void k_tc5_pack(const float* __restrict__ x, int rows, int rows_pad, int d, int KP, int tile_rows,
+                           int is_query, unsigned char* __restrict__ hi, unsigned char* __restrict__ lo) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= rows_pad) return;
+    constexpr int ESZ = MODE == TK_BRUTE_TF32 ? 4 : 2;
+    const int KB = KP * ESZ;
+    const bool real = r < rows;
+    float nrm = 0.f;
+    if (real && !is_query)
+        for (int c = 0; c < d; ++c) nrm = fmaf(x[(long long)r * d + c], x[(long long)r * d + c], nrm);
+    const long long tile_base = (long long)(r / tile_rows) * tile_rows * KB;
+    const int rr = r % tile_rows;
+    for (int c = 0; c < KP; ++c) {
+        float v = 0.f;
+        if (c < d) {
+            v = real ? x[(long long)r * d + c] : 0.f;
+            if (is_query) v = -2.f * v;
+        } else if (c == d) {
+            v = is_query ? (real ? 1.f : 0.f) : (real ? nrm : kT5PadNorm);
+        }
+        const long long off = tile_base + core_offset(rr, c * ESZ, KB);
+        if (MODE == TK_BRUTE_TF32) {
+            *reinterpret_cast<uint32_t*>(hi + off) = to_tf32(v);
+        } else {
+            const __nv_bfloat16 h = __float2bfloat16_rn(v);
+            *reinterpret_cast<__nv_bfloat16*>(hi + off) = h;
+            *reinterpret_cast<__nv_bfloat16*>(lo + off) = __float2bfloat16_rn(v - __bfloat162float(h));
+        }
+    }
+}
+
+struct Tc5Args {
+    const unsigned char* a_hi;  // packed queries, blocks of 128 rows
+    const unsigned char* a_lo;
+    const unsigned char* b_hi;  // packed references, tiles of 256 rows
+    const unsigned char* b_lo;
+    int n, nq, nsplit;
+    float* cand_s;              // [nq, nsplit, 2 * CH]
+    int32_t* cand_i;
+    float* tau;                 // [nq, nsplit]
+    int* err;                   // set when a bounded wait ran out
+};
+
+template <int MODE, int KP, int CH>
+struct Tc5Shape {
+    static constexpr int ESZ = MODE == TK_BRUTE_TF32 ? 4 : 2;
+    static constexpr int KB = KP * ESZ;
+    static constexpr int PL = MODE == TK_BRUTE_TF32 ? 1 : 2;
+    static constexpr uint32_t A_BYTES = uint32_t(kT5Rows) * KB;
+    static constexpr uint32_t B_BYTES = uint32_t(kT5Cols) * KB;
+    static constexpr int KSTEPS = KB / 32;
+    static constexpr size_t SMEM = size_t(PL) * A_BYTES + 2 * size_t(PL) * B_BYTES +
+                                   size_t(CH) * kT5EpiWarps * 32 * (sizeof(float) + sizeof(int32_t));
+};
+
+template <int MODE, int KP, int CH>
+__global__ void __launch_bounds__(kT5Threads, 1) k_tc5_select(const Tc5Args a) {
+    using Sh = Tc5Shape<MODE, KP, CH>;
+    constexpr int PL = Sh::PL, KB = Sh::KB, KSTEPS = Sh::KSTEPS;
+    constexpr uint32_t A_BYTES = Sh::A_BYTES, B_BYTES = Sh::B_BYTES;
+    constexpr uint32_t LBO = 128, SBO = 8 * KB;
+    constexpr int NPROD = MODE == TK_BRUTE_TF32 ? 1 : 3;
+    constexpr uint32_t IDESC = sm100::instr_desc(MODE == TK_BRUTE_TF32 ? 2u : 1u, kT5Rows, kT5Cols);
+    constexpr int NT = kT5EpiWarps * 32;  // epilogue threads (list owners)
+
+    extern __shared__ __align__(1024) unsigned char smem[];
+    unsigned char* sA = smem;                       // [PL][A_BYTES]
+    unsigned char* sB = smem + PL * A_BYTES;        // [2 stages][PL][B_BYTES]
+    float* Ls = reinterpret_cast<float*>(sB + 2 * PL * B_BYTES);  // [CH][NT]
+    int32_t* Li = reinterpret_cast<int32_t*>(Ls + CH * NT);       // [CH][NT]
+    __shared__ __align__(8) uint64_t full_a, full_b[2], mma_done[2], epi_done[2];
+    __shared__ uint32_t tmem_base_sh;
+    __shared__ int abort_sh;
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const long long per0 = ((long long)a.n + a.nsplit - 1) / a.nsplit;
+    const long long per = (per0 + kT5Cols - 1) / kT5Cols * kT5Cols;  // slices start on tile boundaries
+    const int r0 = int(min((long long)a.n, per * blockIdx.y));
+    const int r1 = int(min((long long)a.n, per * (blockIdx.y + 1)));
+    const int ntiles = (r1 - r0 + kT5Cols - 1) / kT5Cols;
+    const int tile0 = r0 / kT5Cols;
+
+    if (tid == 0) {
+        sm100::mbar_init(&full_a, 1);
+        sm100::mbar_init(&full_b[0], 1);
+        sm100::mbar_init(&full_b[1], 1);
+        sm100::mbar_init(&mma_done[0], 1);
+        sm100::mbar_init(&mma_done[1], 1);
+        sm100::mbar_init(&epi_done[0], kT5EpiWarps);
+        sm100::mbar_init(&epi_done[1], kT5EpiWarps);
+        abort_sh = 0;
+        sm100::mbar_fence_init();
+    }
+    if (warp == kT5EpiWarps) sm100::tmem_alloc(&tmem_base_sh, 512);
+    sm100::tc_fence_before();
+    __syncthreads();
+    sm100::tc_fence_after();
+    const uint32_t tmem = tmem_base_sh;
+
+    if (warp == kT5EpiWarps) {
+        // ------------------------------------------------ producer / MMA issuer
+        if (lane == 0 && ntiles > 0) {
+            bool ok = true;
+            sm100::mbar_arrive_expect_tx(&full_a, PL * A_BYTES);
+            sm100::bulk_g2s(sA, a.a_hi + (size_t)blockIdx.x * A_BYTES, A_BYTES, &full_a);
+            if (PL == 2) sm100::bulk_g2s(sA + A_BYTES, a.a_lo + (size_t)blockIdx.x * A_BYTES, A_BYTES, &full_a);
+            for (int t = 0; t < 2 && t < ntiles; ++t) {
+                sm100::mbar_arrive_expect_tx(&full_b[t], PL * B_BYTES);
+                sm100::bulk_g2s(sB + (t * PL) * B_BYTES, a.b_hi + (size_t)(tile0 + t) * B_BYTES, B_BYTES, &full_b[t]);
+                if (PL == 2)
+                    sm100::bulk_g2s(sB + (t * PL + 1) * B_BYTES, a.b_lo + (size_t)(tile0 + t) * B_BYTES, B_BYTES,
+                                    &full_b[t]);
+            }
+            for (int t = 0; t < ntiles && ok; ++t) {
+                const int st = t & 1;
+                const uint32_t ph = (t >> 1) & 1;
+                ok = sm100::mbar_wait(&full_b[st], ph, kT5MaxTries);
+                if (ok && t == 0) ok = sm100::mbar_wait(&full_a, 0, kT5MaxTries);
+                if (ok && t >= 2) ok = sm100::mbar_wait(&epi_done[st], ((t - 2) >> 1) & 1, kT5MaxTries);
+                if (!ok) break;
+                sm100::tc_fence_after();
+                const uint32_t dtm = tmem + uint32_t(st * kT5Cols);
+                const uint32_t a0 = sm100::smem_u32(sA);
+                const uint32_t b0 = sm100::smem_u32(sB + (st * PL) * B_BYTES);
+#pragma unroll
+                for (int ks = 0; ks < KSTEPS; ++ks) {
+#pragma unroll
+                    for (int pr = 0; pr < NPROD; ++pr) {
+                        const uint32_t pa = pr == 2 ? A_BYTES : 0u;  // lo(A) for lo*hi
+                        const uint32_t pb = pr == 1 ? B_BYTES : 0u;  // lo(B) for hi*lo
+                        const uint64_t ad = sm100::smem_desc(a0 + pa + uint32_t(ks) * 256u, LBO, SBO);
+                        const uint64_t bd = sm100::smem_desc(b0 + pb + uint32_t(ks) * 256u, LBO, SBO);
+                        const uint32_t acc = (ks | pr) != 0 ? 1u : 0u;
+                        if (MODE == TK_BRUTE_TF32) sm100::mma_tf32(dtm, ad, bd, IDESC, acc);
+                        else sm100::mma_bf16(dtm, ad, bd, IDESC, acc);
+                    }
+                }
+                sm100::mma_commit(&mma_done[st]);
+                if (t + 2 < ntiles) {
+                    ok = sm100::mbar_wait(&mma_done[st], ph, kT5MaxTries);  // stage st no longer read
+                    if (!ok) break;
+                    sm100::mbar_arrive_expect_tx(&full_b[st], PL * B_BYTES);
+                    sm100::bulk_g2s(sB + (st * PL) * B_BYTES, a.b_hi + (size_t)(tile0 + t + 2) * B_BYTES, B_BYTES,
+                                    &full_b[st]);
+                    if (PL == 2)
+                        sm100::bulk_g2s(sB + (st * PL + 1) * B_BYTES, a.b_lo + (size_t)(tile0 + t + 2) * B_BYTES,
+                                        B_BYTES, &full_b[st]);
+                }
+            }
+            if (!ok) {
+                atomicExch(&abort_sh, 1);
+                atomicExch(a.err, 1);
+            }
+        }
+        __syncwarp();
+    } else {
+        // ------------------------------------------------------- epilogue warps
+        const int quarter = warp & 3, half = warp >> 2;
+        const int th = tid;  // list owner index 0..NT-1
+        int cnt = 0;
+        float tau = __int_as_float(0x7f800000);
+        for (int c = 0; c < CH; ++c) {
+            Ls[c * NT + th] = tau;
+            Li[c * NT + th] = -1;
+        }
+        const uint32_t trow = tmem + (uint32_t(32 * quarter) << 16);
+        for (int t = 0; t < ntiles; ++t) {
+            const int st = t & 1;
+            const uint32_t ph = (t >> 1) & 1;
+            int ok = 1;
+            if (lane == 0) ok = sm100::mbar_wait(&mma_done[st], ph, kT5MaxTries) && !abort_sh;
+            ok = __shfl_sync(0xFFFFFFFFu, ok, 0);
+            if (!ok) {
+                if (lane == 0) {
+                    atomicExch(&abort_sh, 1);
+                    atomicExch(a.err, 1);
+                }
+                break;
+            }
+            sm100::tc_fence_after();
+            const int cbase = r0 + t * kT5Cols + half * (kT5Cols / 2);
+#pragma unroll 1
+            for (int c = 0; c < kT5Cols / 2; c += 16) {
+                float v[16];
+                sm100::tmem_ld16(trow + uint32_t(st * kT5Cols + half * (kT5Cols / 2) + c), v);
+#pragma unroll
+                for (int i = 0; i < 16; ++i) {
+                    const int ref = cbase + c + i;
+                    if (v[i] < tau && ref < r1) {
+                        int pos = cnt < CH ? cnt : CH - 1;
+                        while (pos > 0 && Ls[(pos - 1) * NT + th] > v[i]) {
+                            Ls[pos * NT + th] = Ls[(pos - 1) * NT + th];
+                            Li[pos * NT + th] = Li[(pos - 1) * NT + th];
+                            --pos;
+                        }
+                        Ls[pos * NT + th] = v[i];
+                        Li[pos * NT + th] = ref;
+                        cnt = min(cnt + 1, CH);
+                        if (cnt == CH) tau = Ls[(CH - 1) * NT + th];
+                    }
+                }
+            }
+            sm100::tc_fence_before();
+            __syncwarp();
+            if (lane == 0) sm100::mbar_arrive(&epi_done[st]);
+        }
+        // row's candidates: this thread's list is one half of the row's 2*CH
+        const int row = 32 * quarter + lane;
+        const int q = blockIdx.x * kT5Rows + row;
+        if (q < a.nq) {
+            const long long base = ((long long)q * a.nsplit + blockIdx.y) * (2 * CH) + half * CH;
+            for (int c = 0; c < CH; ++c) {
+                a.cand_s[base + c] = Ls[c * NT + th];
+                a.cand_i[base + c] = Li[c * NT + th];
+            }
+            Ls[0 * NT + th] = cnt == CH ? tau : __int_as_float(0x7f800000);  // reuse slot 0 for the threshold
+        }
+    }
+    // teardown: everyone done with tensor memory
+    sm100::tc_fence_before();
+    __syncthreads();
+    sm100::tc_fence_after();
+    if (warp < 4) {  // one thread per row writes min(tau of both halves)
+        const int row = 32 * warp + lane;
+        const int q = blockIdx.x * kT5Rows + row;
+        if (q < a.nq) {
+            const float t0 = Ls[0 * NT + tid], t1 = Ls[0 * NT + tid + 128];
+            a.tau[(long long)q * a.nsplit + blockIdx.y] = fminf(t0, t1);
+        }
+    }
+    if (warp == kT5EpiWarps) sm100::tmem_dealloc(tmem, 512);
+}
+
 template <int MODE, int KP, int C>
 size_t select_smem_bytes() {
     constexpr int KW = (MODE == TK_BRUTE_TF32) ? KP : KP / 2;
@@ -262,6 +521,7 @@ struct RerankArgs {
     int32_t* out_i;
     int* fail_count;
     int* fail_list;
+    const int* err;       // candidate kernel gave up (bounded wait ran out): certify nothing
 };
 
 // One warp per query: exact distances of the candidates, top-k, certificate.
@@ -297,8 +557,8 @@ __global__ void __launch_bounds__(256) k_tc_rerank(const RerankArgs a) {
     if (lane == 0) {
         double tau = INFINITY;
         for (int s = 0; s < a.nsplit; ++s) tau = fmin(tau, (double)a.tau[(long long)qi * a.nsplit + s]);
-        bool ok = true;
-        if (!isinf(tau)) {
+        bool ok = !(a.err && *a.err);
+        if (ok && !isinf(tau)) {
             const double D = (double)worst.dist();
             double qq = 0.0;
             for (int c = 0; c < a.d; ++c) qq += (double)qrow[c] * (double)qrow[c];
@@ -319,9 +579,20 @@ __global__ void __launch_bounds__(256) k_tc_rerank(const RerankArgs a) {
 }
 
 struct TcWs {
-    size_t a_pack, b_pack, a_lo, b_lo, rnorm, qnorm, cand_s, cand_i, tau, fail_count, fail_list, brute, total;
+    size_t a_pack, b_pack, a_lo, b_lo, rnorm, qnorm, cand_s, cand_i, tau, fail_count, fail_list, brute, err, total;
     int KP, C, nsplit;
+    bool tc5;  // tcgen05 path
 };
+
+// tcgen05 path: K = d + 1 (augmented), padded to the MMA's K step.
+bool tc5_eligible(int d, int k, int mode) {
+    if (k > 32) return false;
+    return mode == TK_BRUTE_TF32 ? (d + 1 <= 40) : (d + 1 <= 48);
+}
+int tc5_kp(int d, int mode) {
+    const int step = mode == TK_BRUTE_TF32 ? 8 : 16;
+    return (d + 1 + step - 1) / step * step;
+}
 
 int tc_kp(int d, int mode) {
     const int step = mode == TK_BRUTE_TF32 ? 8 : 16;
@@ -340,20 +611,36 @@ int tc_over(int k) {
 
 TcWs tc_layout(int64_t n, int64_t nq, int d, int k, int mode, int sms) {
     TcWs w;
-    w.KP = tc_kp(d, mode);
+    w.tc5 = tc5_eligible(d, k, mode);
+    w.KP = w.tc5 ? tc5_kp(d, mode) : tc_kp(d, mode);
     w.C = tc_over(k);
-    const int qblocks = int((nq + kRows - 1) / kRows);
-    int ns = std::max(1, (2 * sms + qblocks - 1) / std::max(1, qblocks));
-    ns = int(std::min<int64_t>(ns, std::max<int64_t>(1, n / (4 * kCols))));
-    w.nsplit = ns;
     const size_t es = mode == TK_BRUTE_TF32 ? 4 : 2;
     size_t o = 0;
-    w.a_pack = o; o += align256(es * size_t(nq) * w.KP);
-    w.b_pack = o; o += align256(es * size_t(n) * w.KP);
-    w.a_lo = o; o += mode == TK_BRUTE_TF32 ? 0 : align256(es * size_t(nq) * w.KP);
-    w.b_lo = o; o += mode == TK_BRUTE_TF32 ? 0 : align256(es * size_t(n) * w.KP);
-    w.rnorm = o; o += align256(4 * size_t(n));
-    w.qnorm = o; o += align256(4 * size_t(nq));
+    if (w.tc5) {
+        const int qblocks = int((nq + kT5Rows - 1) / kT5Rows);
+        int ns = std::max(1, (8 * sms + qblocks / 2) / std::max(1, qblocks));
+        ns = int(std::min<int64_t>({int64_t(ns), int64_t(8), std::max<int64_t>(1, n / (8 * kT5Cols))}));
+        w.nsplit = ns;
+        const size_t nq_pad = size_t(qblocks) * kT5Rows;
+        const size_t n_pad = size_t((n + kT5Cols - 1) / kT5Cols) * kT5Cols;
+        w.a_pack = o; o += align256(es * nq_pad * w.KP);
+        w.b_pack = o; o += align256(es * n_pad * w.KP);
+        w.a_lo = o; o += mode == TK_BRUTE_TF32 ? 0 : align256(es * nq_pad * w.KP);
+        w.b_lo = o; o += mode == TK_BRUTE_TF32 ? 0 : align256(es * n_pad * w.KP);
+        w.rnorm = w.qnorm = o;
+    } else {
+        const int qblocks = int((nq + kRows - 1) / kRows);
+        int ns = std::max(1, (2 * sms + qblocks - 1) / std::max(1, qblocks));
+        ns = int(std::min<int64_t>(ns, std::max<int64_t>(1, n / (4 * kCols))));
+        w.nsplit = ns;
+        w.a_pack = o; o += align256(es * size_t(nq) * w.KP);
+        w.b_pack = o; o += align256(es * size_t(n) * w.KP);
+        w.a_lo = o; o += mode == TK_BRUTE_TF32 ? 0 : align256(es * size_t(nq) * w.KP);
+        w.b_lo = o; o += mode == TK_BRUTE_TF32 ? 0 : align256(es * size_t(n) * w.KP);
+        w.rnorm = o; o += align256(4 * size_t(n));
+        w.qnorm = o; o += align256(4 * size_t(nq));
+    }
+    w.err = o; o += 256;
     w.cand_s = o; o += align256(4 * size_t(nq) * w.nsplit * w.C);
     w.cand_i = o; o += align256(4 * size_t(nq) * w.nsplit * w.C);
     w.tau = o; o += align256(4 * size_t(nq) * w.nsplit);
@@ -369,6 +656,47 @@ int sm_count_now() {
     cudaGetDevice(&dev);
     if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v < 1) v = 1;
     return v;
+}
+
+template <int MODE, int KP, int CH>
+int launch_tc5(const Tc5Args& a, int qblocks, cudaStream_t s) {
+    using Sh = Tc5Shape<MODE, KP, CH>;
+    const void* fn = reinterpret_cast<const void*>(&k_tc5_select<MODE, KP, CH>);
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(Sh::SMEM));
+    if (e != cudaSuccess) return fail(TK_ECUDA, std::string("tcgen05 select smem: ") + cudaGetErrorString(e));
+    k_tc5_select<MODE, KP, CH><<<dim3(qblocks, a.nsplit), kT5Threads, Sh::SMEM, s>>>(a);
+    return TK_OK;
+}
+
+template <int MODE, int KP>
+int tc5_dispatch_ch(const Tc5Args& a, int CH, int qblocks, cudaStream_t s) {
+    switch (CH) {
+        case 8: return launch_tc5<MODE, KP, 8>(a, qblocks, s);
+        case 16: return launch_tc5<MODE, KP, 16>(a, qblocks, s);
+        case 32: return launch_tc5<MODE, KP, 32>(a, qblocks, s);
+        default: return fail(TK_EUNSUPPORTED, "tcgen05 path: k <= 32");
+    }
+}
+
+int tc5_dispatch(const Tc5Args& a, int mode, int KP, int CH, int qblocks, cudaStream_t s) {
+    if (mode == TK_BRUTE_TF32) {
+        switch (KP) {
+            case 8: return tc5_dispatch_ch<TK_BRUTE_TF32, 8>(a, CH, qblocks, s);
+            case 16: return tc5_dispatch_ch<TK_BRUTE_TF32, 16>(a, CH, qblocks, s);
+            case 24: return tc5_dispatch_ch<TK_BRUTE_TF32, 24>(a, CH, qblocks, s);
+            case 32: return tc5_dispatch_ch<TK_BRUTE_TF32, 32>(a, CH, qblocks, s);
+            case 40: return tc5_dispatch_ch<TK_BRUTE_TF32, 40>(a, CH, qblocks, s);
+            default: break;
+        }
+    } else {
+        switch (KP) {
+            case 16: return tc5_dispatch_ch<TK_BRUTE_BF16_SPLIT, 16>(a, CH, qblocks, s);
+            case 32: return tc5_dispatch_ch<TK_BRUTE_BF16_SPLIT, 32>(a, CH, qblocks, s);
+            case 48: return tc5_dispatch_ch<TK_BRUTE_BF16_SPLIT, 48>(a, CH, qblocks, s);
+            default: break;
+        }
+    }
+    return fail(TK_EUNSUPPORTED, "tcgen05 path: unsupported depth");
 }
 
 template <int MODE, int KP, int C>
@@ -420,8 +748,43 @@ int run_brute_tc(const float* ref, int64_t n, const float* q, int64_t nq, int d,
     if (!ws || ws_bytes < w.total) return fail(TK_EWORKSPACE, "workspace too small");
     char* p = static_cast<char*>(ws);
     const int n32 = int(n), nq32 = int(nq);
-    // 1. pack
-    if (mode == TK_BRUTE_TF32) {
+    cudaError_t e0 = cudaMemsetAsync(p + w.err, 0, sizeof(int), s);
+    if (e0 != cudaSuccess) return fail(TK_ECUDA, std::string("memset: ") + cudaGetErrorString(e0));
+    int crc = TK_OK;
+    int C_eff = w.C;
+    if (w.tc5) {
+        // 1-2. pack into the core-matrix layout and run the tcgen05 candidate kernel
+        const int qblocks = (nq32 + kT5Rows - 1) / kT5Rows;
+        const int n_pad = int((n + kT5Cols - 1) / kT5Cols) * kT5Cols;
+        unsigned char* ahi = reinterpret_cast<unsigned char*>(p + w.a_pack);
+        unsigned char* alo = reinterpret_cast<unsigned char*>(p + w.a_lo);
+        unsigned char* bhi = reinterpret_cast<unsigned char*>(p + w.b_pack);
+        unsigned char* blo = reinterpret_cast<unsigned char*>(p + w.b_lo);
+        const int nq_pad = qblocks * kT5Rows;
+        if (mode == TK_BRUTE_TF32) {
+            k_tc5_pack<TK_BRUTE_TF32><<<(nq_pad + 255) / 256, 256, 0, s>>>(q, nq32, nq_pad, d, w.KP, kT5Rows, 1, ahi, alo);
+            k_tc5_pack<TK_BRUTE_TF32><<<(n_pad + 255) / 256, 256, 0, s>>>(ref, n32, n_pad, d, w.KP, kT5Cols, 0, bhi, blo);
+        } else {
+            k_tc5_pack<TK_BRUTE_BF16_SPLIT><<<(nq_pad + 255) / 256, 256, 0, s>>>(q, nq32, nq_pad, d, w.KP, kT5Rows, 1,
+                                                                               ahi, alo);
+            k_tc5_pack<TK_BRUTE_BF16_SPLIT><<<(n_pad + 255) / 256, 256, 0, s>>>(ref, n32, n_pad, d, w.KP, kT5Cols, 0,
+                                                                              bhi, blo);
+        }
+        Tc5Args t5{};
+        t5.a_hi = ahi;
+        t5.a_lo = alo;
+        t5.b_hi = bhi;
+        t5.b_lo = blo;
+        t5.n = n32;
+        t5.nq = nq32;
+        t5.nsplit = w.nsplit;
+        t5.cand_s = reinterpret_cast<float*>(p + w.cand_s);
+        t5.cand_i = reinterpret_cast<int32_t*>(p + w.cand_i);
+        t5.tau = reinterpret_cast<float*>(p + w.tau);
+        t5.err = reinterpret_cast<int*>(p + w.err);
+        crc = tc5_dispatch(t5, mode, w.KP, w.C / 2, qblocks, s);
+        if (crc != TK_OK) return crc;
+    } else if (mode == TK_BRUTE_TF32) {
         k_tc_pack<TK_BRUTE_TF32><<<(nq32 + 255) / 256, 256, 0, s>>>(q, nq32, d, w.KP, reinterpret_cast<uint32_t*>(p + w.a_pack),
                                                                   nullptr, nullptr, reinterpret_cast<float*>(p + w.qnorm));
         k_tc_pack<TK_BRUTE_TF32><<<(n32 + 255) / 256, 256, 0, s>>>(ref, n32, d, w.KP, reinterpret_cast<uint32_t*>(p + w.b_pack),
@@ -452,9 +815,11 @@ int run_brute_tc(const float* ref, int64_t n, const float* q, int64_t nq, int d,
     a.cand_i = reinterpret_cast<int32_t*>(p + w.cand_i);
     a.tau = reinterpret_cast<float*>(p + w.tau);
     const int qblocks = (nq32 + kRows - 1) / kRows;
-    int rc = mode == TK_BRUTE_TF32 ? dispatch_kp<TK_BRUTE_TF32>(a, qblocks, s)
-                                   : dispatch_kp<TK_BRUTE_BF16_SPLIT>(a, qblocks, s);
-    if (rc != TK_OK) return rc;
+    if (!w.tc5) {
+        crc = mode == TK_BRUTE_TF32 ? dispatch_kp<TK_BRUTE_TF32>(a, qblocks, s)
+                                    : dispatch_kp<TK_BRUTE_BF16_SPLIT>(a, qblocks, s);
+        if (crc != TK_OK) return crc;
+    }
     // 3. exact re-rank + certificate
     cudaError_t e = cudaMemsetAsync(p + w.fail_count, 0, sizeof(int), s);
     if (e != cudaSuccess) return fail(TK_ECUDA, std::string("memset: ") + cudaGetErrorString(e));
@@ -471,12 +836,13 @@ int run_brute_tc(const float* ref, int64_t n, const float* q, int64_t nq, int d,
     ra.cand_i = a.cand_i;
     ra.tau = a.tau;
     const double u = 1.0 / 16777216.0;
-    ra.eps_dot = mode == TK_BRUTE_TF32 ? (1.0 / 1024.0 + 1.0 / 4194304.0 + d * 2.0 * u)
-                                       : (3.1 / 65536.0 + 3.0 * d * 2.0 * u);
+    ra.eps_dot = mode == TK_BRUTE_TF32 ? (1.0 / 1024.0 + 1.0 / 4194304.0 + (d + 2) * 2.0 * u)
+                                       : (3.1 / 65536.0 + 3.0 * (d + 2) * 2.0 * u);
     ra.out_d = dists;
     ra.out_i = idx;
     ra.fail_count = reinterpret_cast<int*>(p + w.fail_count);
     ra.fail_list = reinterpret_cast<int*>(p + w.fail_list);
+    ra.err = reinterpret_cast<const int*>(p + w.err);
     const int rb = (nq32 + 7) / 8;
     if (k <= 32) k_tc_rerank<1><<<rb, 256, 0, s>>>(ra);
     else k_tc_rerank<2><<<rb, 256, 0, s>>>(ra);
