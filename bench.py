@@ -209,12 +209,12 @@ def run_ours(args, rank, world):
     if args.levels and args.tpq:
         from torch_kdtree_gb300.autotune import Choice
         ch = Choice(levels=args.levels, threads_per_query=args.tpq, ms=float("nan"), plain_levels=plain.levels,
-                    table=[])
+                    table=[], prune_boxes=args.boxes)
     else:
         ch = autotune(ref, q, K_NN, use_cache=False)
     tune_s = time.perf_counter() - t0
     t0 = time.perf_counter()
-    chosen = tk.build_kd_tree(ref, levels=ch.levels, query_opts=QueryOpts.make(threads_per_query=ch.threads_per_query))
+    chosen = tk.build_kd_tree(ref, levels=ch.levels, query_opts=ch.opts())
     build_chosen_s = time.perf_counter() - t0
 
     if args.profile:
@@ -284,7 +284,7 @@ def run_ours(args, rank, world):
     ke.record()  # materialise the events
     torch.cuda.synchronize()
     kopts = QueryOpts.make(threads_per_query=ch.threads_per_query, kernel_start_event=ks.cuda_event,
-                           kernel_stop_event=ke.cuda_event)
+                           kernel_stop_event=ke.cuda_event, prune_boxes=ch.prune_boxes)
     kern_ms = []
     for _ in range(max(3, args.steps)):
         flush.zero_()
@@ -339,6 +339,7 @@ def run_ours(args, rank, world):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded numpy, shapes and distributions of the workload)",
         "config": {"workload": WORKLOAD, "levels": ch.levels, "threads_per_query": ch.threads_per_query,
+                   "prune_boxes": ch.prune_boxes,
                    "graph_captured": True, "l2": f"flushed between steps ({L2_FLUSH_BYTES >> 20} MiB write)",
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                    "tree_build_s": {"plain": build_plain_s, "chosen": build_chosen_s}, "autotune_s": tune_s},
@@ -542,6 +543,16 @@ def run_brute_tc(args):
     torch.cuda.set_device(dev)
     k = 32
     out = {}
+    if args.profile:
+        # one tensor-core call on a reduced query set (for ncu captures)
+        ref_np, q_np = tensor_core_brute(d=32, n_query=16384)
+        ref = torch.from_numpy(ref_np).to(dev)
+        q = torch.from_numpy(q_np).to(dev)
+        dd = torch.empty(len(q), k, device=dev)
+        ii = torch.empty(len(q), k, dtype=torch.int32, device=dev)
+        nn_distance_raw(ref, q, k, dd, ii, "tf32")
+        torch.cuda.synchronize()
+        return
     for d in (8, 32):
         ref_np, q_np = tensor_core_brute(d=d)
         ref = torch.from_numpy(ref_np).to(dev)
@@ -586,6 +597,7 @@ def main():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--levels", type=int, default=0, help="chosen tree depth (skips the autotuner with --tpq)")
     p.add_argument("--tpq", type=int, default=0, help="chosen lanes per query (skips the autotuner with --levels)")
+    p.add_argument("--boxes", type=int, default=1, help="chosen: prune with node bounding boxes (with --levels/--tpq)")
     p.add_argument("--profile", action="store_true", help="run one chosen and one plain query only (for ncu)")
     p.add_argument("--workload", default="kd", choices=["kd", "batched", "backward", "brute", "brute_tc"],
                    help="kd (default): the headline large single-cloud query; the others measure the "

@@ -96,6 +96,7 @@ typedef struct tk_query_opts {
     int32_t blocks_per_sm;     /* 0 = as many as fit */
     void* kernel_start_event;  /* optional cudaEvent_t recorded right before the KD kernel */
     void* kernel_stop_event;   /* optional cudaEvent_t recorded right after it */
+    int32_t prune_boxes;       /* -1 = auto (on), 0 = split planes only, 1 = also node bounding boxes */
 } tk_query_opts;
 
 /* Bytes of device scratch tk_tree_query needs for nq queries. */
@@ -149,9 +150,10 @@ int64_t tk_batch_output_size(const tk_batch* batch);
 /* All clouds in one persistent launch fed by a global work counter (plus
  * the binning kernels).  Device work only, no host synchronisation and no
  * allocation: it can be captured in a CUDA graph.  threads_per_query: 0 =
- * auto, 1 (max k <= 16) or 8. */
+ * auto, 1 (max k <= 16) or 8.  prune_boxes: 0 = split planes only, 1 = also
+ * node bounding boxes (as in tk_query_opts). */
 int tk_batch_query(const tk_batch* batch, const void* q, void* dists, int32_t* idx, int threads_per_query,
-                   void* workspace, size_t workspace_bytes, void* stream);
+                   int prune_boxes, void* workspace, size_t workspace_bytes, void* stream);
 
 /* -------------------------------------------------------- brute force -- */
 

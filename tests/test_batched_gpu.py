@@ -15,13 +15,14 @@ def make_clouds(n_clouds, lo, hi, seed):
 
 
 @pytest.mark.parametrize("tpq", [0, 8])
-def test_batch_matches_per_cloud_and_oracle(tpq, oracle):
+@pytest.mark.parametrize("boxes", [False, True])
+def test_batch_matches_per_cloud_and_oracle(tpq, boxes, oracle):
     from torch_kdtree_gb300.batched import BatchedKDTrees
     clouds = make_clouds(24, 50, 20000, seed=3)
     refs = [torch.from_numpy(r).to(cuda) for r, _, _ in clouds]
     qs = [torch.from_numpy(q).to(cuda) for _, q, _ in clouds]
     ks = [k for _, _, k in clouds]
-    b = BatchedKDTrees(refs, ks, [q.shape[0] for q in qs], threads_per_query=tpq)
+    b = BatchedKDTrees(refs, ks, [q.shape[0] for q in qs], threads_per_query=tpq, prune_boxes=boxes)
     d_b, i_b = b.query(qs)
     b.query_each(qs)
     d_e, i_e = b.split(b.out_dists), b.split(b.out_idx)

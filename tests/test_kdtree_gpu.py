@@ -53,9 +53,10 @@ def test_launch_shapes_give_identical_results(tpq, k, oracle):
     q = (rng.standard_normal((3000, 3)) * 1.2).astype(np.float32)
     bd, bi = oracle.brute(ref, q, k)
     for binq in (0, 1):
-        d, i = gpu_query(ref, q, k, levels=9, threads_per_query=tpq, bin_queries=binq)
-        np.testing.assert_array_equal(d, bd)
-        np.testing.assert_array_equal(i, bi)
+        for boxes in (0, 1):
+            d, i = gpu_query(ref, q, k, levels=9, threads_per_query=tpq, bin_queries=binq, prune_boxes=boxes)
+            np.testing.assert_array_equal(d, bd)
+            np.testing.assert_array_equal(i, bi)
 
 
 @pytest.mark.parametrize("levels", [1, 2, 3, 7, 11, 13, 14])
@@ -65,9 +66,10 @@ def test_any_tree_depth_gives_identical_results(levels, oracle):
     q = (rng.random((2500, 3)) * 1.2 - 0.1).astype(np.float32)
     bd, bi = oracle.brute(ref, q, 16)
     for smem in (0, 5, 12):
-        d, i = gpu_query(ref, q, 16, levels=levels, smem_levels=smem)
-        np.testing.assert_array_equal(d, bd)
-        np.testing.assert_array_equal(i, bi)
+        for boxes in (0, 1):
+            d, i = gpu_query(ref, q, 16, levels=levels, smem_levels=smem, prune_boxes=boxes)
+            np.testing.assert_array_equal(d, bd)
+            np.testing.assert_array_equal(i, bi)
 
 
 @pytest.mark.parametrize("dtype", [np.float32, np.float64])

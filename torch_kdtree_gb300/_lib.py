@@ -49,13 +49,13 @@ class QueryOpts(ctypes.Structure):
     _fields_ = [("threads_per_query", ctypes.c_int32), ("bin_queries", ctypes.c_int32),
                 ("smem_levels", ctypes.c_int32), ("block_threads", ctypes.c_int32),
                 ("blocks_per_sm", ctypes.c_int32), ("kernel_start_event", ctypes.c_void_p),
-                ("kernel_stop_event", ctypes.c_void_p)]
+                ("kernel_stop_event", ctypes.c_void_p), ("prune_boxes", ctypes.c_int32)]
 
     @classmethod
     def make(cls, threads_per_query=0, bin_queries=-1, smem_levels=-1, block_threads=0, blocks_per_sm=0,
-             kernel_start_event=None, kernel_stop_event=None):
+             kernel_start_event=None, kernel_stop_event=None, prune_boxes=-1):
         return cls(threads_per_query, bin_queries, smem_levels, block_threads, blocks_per_sm,
-                   kernel_start_event, kernel_stop_event)
+                   kernel_start_event, kernel_stop_event, prune_boxes)
 
 
 _vp = ctypes.c_void_p
@@ -82,7 +82,7 @@ SIGNATURES = {
     "tk_batch_destroy": (_int, [_vp]),
     "tk_batch_workspace_size": (_sz, [_vp]),
     "tk_batch_output_size": (_i64, [_vp]),
-    "tk_batch_query": (_int, [_vp, _vp, _vp, _vp, _int, _vp, _sz, _vp]),
+    "tk_batch_query": (_int, [_vp, _vp, _vp, _vp, _int, _int, _vp, _sz, _vp]),
     "tk_nn_distance_workspace_size": (_sz, [_i64, _i64, _int, _int, _int, _int]),
     "tk_nn_distance": (_int, [_vp, _i64, _vp, _i64, _int, _int, _int, _int, _vp, _vp, _vp, _sz, _vp]),
     "tk_tree_query_noalloc": (_int, [_vp, _vp, _i64, _int, _vp, _vp, ctypes.POINTER(QueryOpts), _vp]),

@@ -31,7 +31,11 @@ class Choice:
     threads_per_query: int
     ms: float
     plain_levels: int
-    table: list  # (levels, lanes, ms) of every timed candidate
+    table: list  # (levels, lanes, boxes, ms) of every timed candidate
+    prune_boxes: int = 1
+
+    def opts(self) -> QueryOpts:
+        return QueryOpts.make(threads_per_query=self.threads_per_query, prune_boxes=self.prune_boxes)
 
 
 def _key(n, nq, k, d, dtype, device) -> str:
@@ -100,12 +104,14 @@ def autotune(points_ref: torch.Tensor, queries: torch.Tensor, k: int,
         for g in lanes:
             if g * 16 < k:  # a lane holds at most 16 list entries
                 continue
-            ms = time_query(tree, q, k, QueryOpts.make(threads_per_query=g), reps)
-            table.append((L, g, ms))
-            if best is None or ms < best[2]:
-                best = (L, g, ms)
+            for boxes in (1, 0):
+                ms = time_query(tree, q, k, QueryOpts.make(threads_per_query=g, prune_boxes=boxes), reps)
+                table.append((L, g, boxes, ms))
+                if best is None or ms < best[3]:
+                    best = (L, g, boxes, ms)
         del tree
-    ch = Choice(levels=best[0], threads_per_query=best[1], ms=best[2], plain_levels=L0, table=table)
+    ch = Choice(levels=best[0], threads_per_query=best[1], ms=best[3], plain_levels=L0, table=table,
+                prune_boxes=best[2])
     if use_cache:
         cache[key] = asdict(ch)
         _store_cache(cache)
@@ -115,4 +121,4 @@ def autotune(points_ref: torch.Tensor, queries: torch.Tensor, k: int,
 def build_tuned_kd_tree(points_ref: torch.Tensor, queries: torch.Tensor, k: int, **kw) -> TorchKDTree:
     """build_kd_tree with the autotuned depth and lanes per query."""
     ch = autotune(points_ref, queries, k, **kw)
-    return build_kd_tree(points_ref, levels=ch.levels, query_opts=QueryOpts.make(threads_per_query=ch.threads_per_query))
+    return build_kd_tree(points_ref, levels=ch.levels, query_opts=ch.opts())

@@ -23,7 +23,7 @@ from .nn_distance import TorchKDTree, _stream_ptr, _workspace, build_kd_tree, kn
 class BatchedKDTrees:
     def __init__(self, clouds: Sequence[torch.Tensor], ks: Sequence[int], query_counts: Sequence[int],
                  levels: Optional[Sequence[Optional[int]]] = None, device: Optional[torch.device] = None,
-                 threads_per_query: int = 0):
+                 threads_per_query: int = 0, prune_boxes: bool = False):
         if not (len(clouds) == len(ks) == len(query_counts)) or not clouds:
             raise ValueError("clouds, ks and query_counts must be non-empty and of equal length")
         device = torch.device(device) if device is not None else clouds[0].device
@@ -39,6 +39,7 @@ class BatchedKDTrees:
         self.dtype = self.trees[0].dtype
         self.dims = self.trees[0].dims
         self.threads_per_query = int(threads_per_query)
+        self.prune_boxes = int(bool(prune_boxes))
         handles = (ctypes.c_void_p * len(self.trees))(*[t._tree.handle.value for t in self.trees])
         qc = (ctypes.c_int64 * len(self.trees))(*self.query_counts)
         kk = (ctypes.c_int32 * len(self.trees))(*self.ks)
@@ -69,7 +70,7 @@ class BatchedKDTrees:
         if not q_flat.is_contiguous() or q_flat.device != self.device:
             raise AssertionError("queries must be contiguous on the batch's device")
         check(LIB.tk_batch_query(self._h, q_flat.data_ptr(), out_dists.data_ptr(), out_idx.data_ptr(),
-                                 self.threads_per_query, self._ws.data_ptr(), self.ws_bytes,
+                                 self.threads_per_query, self.prune_boxes, self._ws.data_ptr(), self.ws_bytes,
                                  _stream_ptr(self.device)))
 
     def split(self, flat: torch.Tensor) -> List[torch.Tensor]:

@@ -29,6 +29,7 @@ struct CloudDesc {
     const PointRec<T>* pts;
     const T* medians;
     const int32_t* leaf_off;
+    const PointRec<T>* boxes;  // null: prune with split planes only
     long long out_off;  // element offset of the cloud's [nq_c, k_c] block in the outputs
     int levels;
     int k;
@@ -47,6 +48,7 @@ struct BatchArgs {
     T* out_d;
     int32_t* out_i;
     int* work;
+    int use_boxes;
 };
 
 __device__ __forceinline__ int cloud_of(const long long* prefix, int n_clouds, long long qi) {
@@ -83,7 +85,7 @@ __global__ void k_batch_bin_count(const BatchArgs<T> a, int* counts, int* bin_of
 template <typename T, int D, int G, int R>
 __device__ __forceinline__ void batch_search(const CloudDesc<T>& cd, const T (&q)[D], long long local,
                                              const BatchArgs<T>& a, unsigned gmask, int gl, int gbase) {
-    const TreeView<T> tv{cd.pts, cd.medians, cd.leaf_off, cd.levels, 0, nullptr};
+    const TreeView<T> tv{cd.pts, cd.medians, cd.leaf_off, cd.levels, 0, nullptr, a.use_boxes ? cd.boxes : nullptr};
     const long long o = cd.out_off + local * cd.k;
     kd_search<T, D, G, R>(tv, q, cd.k, a.out_d + o, a.out_i + o, gmask, gl, gbase);
 }
@@ -190,6 +192,7 @@ int upload_descs(tk_batch* b, const tk_tree* const* trees, const int64_t* q_coun
         d.pts = static_cast<const PointRec<T>*>(t->d_pts);
         d.medians = static_cast<const T*>(t->d_medians);
         d.leaf_off = t->d_leaf_off;
+        d.boxes = static_cast<const PointRec<T>*>(t->d_boxes);
         d.out_off = b->out_off[c];
         d.levels = t->levels;
         d.k = ks[c];
@@ -210,7 +213,7 @@ int upload_descs(tk_batch* b, const tk_tree* const* trees, const int64_t* q_coun
 }
 
 template <typename T, int D>
-int run_batch(const tk_batch* b, const T* q, T* dists, int32_t* idx, int G, char* ws, cudaStream_t s) {
+int run_batch(const tk_batch* b, const T* q, T* dists, int32_t* idx, int G, int boxes, char* ws, cudaStream_t s) {
     const BatchWs w = batch_ws(b);
     BatchArgs<T> a;
     a.desc = static_cast<const CloudDesc<T>*>(b->d_desc);
@@ -221,6 +224,7 @@ int run_batch(const tk_batch* b, const T* q, T* dists, int32_t* idx, int G, char
     a.out_d = dists;
     a.out_i = idx;
     a.work = reinterpret_cast<int*>(ws + w.counter);
+    a.use_boxes = boxes;
     int* counts = reinterpret_cast<int*>(ws + w.counts);
     int* bin_of = reinterpret_cast<int*>(ws + w.bin_of);
     int* pos_of = reinterpret_cast<int*>(ws + w.pos_of);
@@ -318,7 +322,7 @@ size_t tk_batch_workspace_size(const tk_batch* b) { return b ? batch_ws(b).total
 int64_t tk_batch_output_size(const tk_batch* b) { return b ? b->total_out : 0; }
 
 int tk_batch_query(const tk_batch* b, const void* q, void* dists, int32_t* idx, int threads_per_query,
-                   void* workspace, size_t workspace_bytes, void* stream) {
+                   int prune_boxes, void* workspace, size_t workspace_bytes, void* stream) {
     clear_error();
     if (!b) return fail(TK_EINVAL, "batch is null");
     if (b->total_q == 0) return TK_OK;
@@ -332,15 +336,15 @@ int tk_batch_query(const tk_batch* b, const void* q, void* dists, int32_t* idx, 
     char* ws = static_cast<char*>(workspace);
     if (b->dtype == TK_F32) {
         switch (b->dims) {
-            case 1: return run_batch<float, 1>(b, static_cast<const float*>(q), static_cast<float*>(dists), idx, G, ws, s);
-            case 2: return run_batch<float, 2>(b, static_cast<const float*>(q), static_cast<float*>(dists), idx, G, ws, s);
-            default: return run_batch<float, 3>(b, static_cast<const float*>(q), static_cast<float*>(dists), idx, G, ws, s);
+            case 1: return run_batch<float, 1>(b, static_cast<const float*>(q), static_cast<float*>(dists), idx, G, prune_boxes != 0, ws, s);
+            case 2: return run_batch<float, 2>(b, static_cast<const float*>(q), static_cast<float*>(dists), idx, G, prune_boxes != 0, ws, s);
+            default: return run_batch<float, 3>(b, static_cast<const float*>(q), static_cast<float*>(dists), idx, G, prune_boxes != 0, ws, s);
         }
     }
     switch (b->dims) {
-        case 1: return run_batch<double, 1>(b, static_cast<const double*>(q), static_cast<double*>(dists), idx, G, ws, s);
-        case 2: return run_batch<double, 2>(b, static_cast<const double*>(q), static_cast<double*>(dists), idx, G, ws, s);
-        default: return run_batch<double, 3>(b, static_cast<const double*>(q), static_cast<double*>(dists), idx, G, ws, s);
+        case 1: return run_batch<double, 1>(b, static_cast<const double*>(q), static_cast<double*>(dists), idx, G, prune_boxes != 0, ws, s);
+        case 2: return run_batch<double, 2>(b, static_cast<const double*>(q), static_cast<double*>(dists), idx, G, prune_boxes != 0, ws, s);
+        default: return run_batch<double, 3>(b, static_cast<const double*>(q), static_cast<double*>(dists), idx, G, prune_boxes != 0, ws, s);
     }
 }
 

@@ -90,11 +90,33 @@ __global__ void __launch_bounds__(256) k_brute(const BruteArgs<T> a) {
         }
         __syncthreads();
         if (active) {
-            for (int j0 = 0; j0 < len; j0 += G) {
-                const int j = j0 + gl;
-                Key<T> mine = Key<T>::sentinel();
-                if (j < len) mine = Key<T>::make(sqdist_padded<T, DP>(q, tile + j * DP), uint32_t(t0 + j));
-                worst = offer<T, G, R>(list, mine, worst, gmask, gl, gbase);
+            // four references per lane step: four independent accumulation chains
+            constexpr int U = DP <= 4 ? 1 : ((DP > 32 || R >= 16) ? 2 : 4);
+            for (int j0 = 0; j0 < len; j0 += G * U) {
+                T acc[U];
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    const int j = min(j0 + u * G + gl, TR - 1);  // rows past len are padding zeros
+                    const T* r = tile + j * DP;
+                    const T d0 = sub_rn(q[0], r[0]);
+                    acc[u] = mul_rn(d0, d0);
+                }
+#pragma unroll
+                for (int c = 1; c < DP; ++c) {
+#pragma unroll
+                    for (int u = 0; u < U; ++u) {
+                        const int j = min(j0 + u * G + gl, TR - 1);
+                        const T dc = sub_rn(q[c], tile[j * DP + c]);
+                        acc[u] = add_rn(acc[u], mul_rn(dc, dc));
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    const int j = j0 + u * G + gl;
+                    Key<T> mine = Key<T>::sentinel();
+                    if (j < len) mine = Key<T>::make(acc[u], uint32_t(t0 + j));
+                    worst = offer<T, G, R>(list, mine, worst, gmask, gl, gbase);
+                }
             }
         }
     }

@@ -256,7 +256,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc_select(const TcArgs a) {
 // become candidates.
 constexpr int kT5Rows = 128;   // M (queries per block)
 constexpr int kT5Cols = 256;   // N (references per tile)
-constexpr int kT5EpiWarps = 8; // two warps per 32-lane quarter of the accumulator, one column half each
+constexpr int kT5EpiWarps = 16; // 4 per 32-lane quarter of the accumulator when reading tensor memory
+constexpr int kT5Chunk = 64;    // accumulator columns moved to shared memory per step
+constexpr int kT5TStride = kT5Chunk + 4;  // transposed tile row stride (floats), bank-conflict free
 constexpr int kT5Threads = 32 * (kT5EpiWarps + 1);
 constexpr float kT5PadNorm = 1e30f;
 constexpr uint32_t kT5MaxTries = 1u << 22;  // bounded mbarrier polls
@@ -311,6 +313,46 @@ struct Tc5Args {
     int* err;                   // set when a bounded wait ran out
 };
 
+// Score keys: order-preserving uint32 image of the float score (negative
+// scores included) in the high word, reference index in the low word.
+__device__ __forceinline__ unsigned long long score_key(float sc, uint32_t idx) {
+    uint32_t u = __float_as_uint(sc);
+    u = (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+    return (static_cast<unsigned long long>(u) << 32) | idx;
+}
+__device__ __forceinline__ float key_score(unsigned long long key) {
+    const uint32_t u = uint32_t(key >> 32);
+    return __uint_as_float((u & 0x80000000u) ? (u & 0x7FFFFFFFu) : ~u);
+}
+constexpr unsigned long long kScoreSentinel = (0xFF800000ull << 32) | 0xFFFFFFFFull;  // score +inf
+
+// A row's over-fetch list of up to 32 * R keys spread over a warp (slot s on
+// lane s % 32, register s / 32; the first 32 R - C slots are padding below
+// every key), as TopK in tk_device.cuh.
+template <int R>
+struct RowList {
+    unsigned long long slot[R];
+    __device__ __forceinline__ void init(int C, int lane) {
+#pragma unroll
+        for (int r = 0; r < R; ++r) slot[r] = (r * 32 + lane < 32 * R - C) ? 0ull : kScoreSentinel;
+    }
+    __device__ __forceinline__ void insert(unsigned long long c, int lane) {
+        unsigned long long nw[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const unsigned long long old = slot[r];
+            const unsigned long long up = __shfl_up_sync(0xFFFFFFFFu, old, 1);
+            const unsigned long long wrap = r > 0 ? __shfl_sync(0xFFFFFFFFu, slot[r - 1], 31) : 0ull;
+            const unsigned long long prev = lane == 0 ? wrap : up;
+            const bool has_prev = !(lane == 0 && r == 0);
+            nw[r] = old <= c ? old : ((!has_prev || prev <= c) ? c : prev);
+        }
+#pragma unroll
+        for (int r = 0; r < R; ++r) slot[r] = nw[r];
+    }
+    __device__ __forceinline__ unsigned long long worst() const { return __shfl_sync(0xFFFFFFFFu, slot[R - 1], 31); }
+};
+
 template <int MODE, int KP, int CH>
 struct Tc5Shape {
     static constexpr int ESZ = MODE == TK_BRUTE_TF32 ? 4 : 2;
@@ -320,7 +362,9 @@ struct Tc5Shape {
     static constexpr uint32_t B_BYTES = uint32_t(kT5Cols) * KB;
     static constexpr int KSTEPS = KB / 32;
     static constexpr size_t SMEM = size_t(PL) * A_BYTES + 2 * size_t(PL) * B_BYTES +
-                                   size_t(CH) * kT5EpiWarps * 32 * (sizeof(float) + sizeof(int32_t));
+                                   2 * size_t(kT5Rows) * kT5TStride * sizeof(float) +  // transposed scores
+                                   size_t(kT5Rows) * sizeof(float) +                  // row thresholds
+                                   2 * size_t(kT5Rows) * 4;                           // hit bytes per column group
 };
 
 template <int MODE, int KP, int CH>
@@ -336,11 +380,16 @@ __global__ void __launch_bounds__(kT5Threads, 1) k_tc5_select(const Tc5Args a) {
     extern __shared__ __align__(1024) unsigned char smem[];
     unsigned char* sA = smem;                       // [PL][A_BYTES]
     unsigned char* sB = smem + PL * A_BYTES;        // [2 stages][PL][B_BYTES]
-    float* Ls = reinterpret_cast<float*>(sB + 2 * PL * B_BYTES);  // [CH][NT]
-    int32_t* Li = reinterpret_cast<int32_t*>(Ls + CH * NT);       // [CH][NT]
+    float* sT = reinterpret_cast<float*>(sB + 2 * PL * B_BYTES);  // [2][kT5Rows][kT5TStride] transposed scores
+    float* sThr = sT + 2 * kT5Rows * kT5TStride;                     // [kT5Rows] current list threshold per row
+    uint32_t* sHit = reinterpret_cast<uint32_t*>(sThr + kT5Rows);    // [2][kT5Rows] one byte per column group
     __shared__ __align__(8) uint64_t full_a, full_b[2], mma_done[2], epi_done[2];
     __shared__ uint32_t tmem_base_sh;
     __shared__ int abort_sh;
+    constexpr int C = 2 * CH;                 // over-fetch per row and slice
+    constexpr int R = C <= 32 ? 1 : C / 32;   // list registers per lane
+    constexpr int ROWS_PER_WARP = kT5Rows / kT5EpiWarps;
+    constexpr int NEPI = 32 * kT5EpiWarps;
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const long long per0 = ((long long)a.n + a.nsplit - 1) / a.nsplit;
@@ -425,79 +474,130 @@ __global__ void __launch_bounds__(kT5Threads, 1) k_tc5_select(const Tc5Args a) {
         __syncwarp();
     } else {
         // ------------------------------------------------------- epilogue warps
-        const int quarter = warp & 3, half = warp >> 2;
-        const int th = tid;  // list owner index 0..NT-1
-        int cnt = 0;
-        float tau = __int_as_float(0x7f800000);
-        for (int c = 0; c < CH; ++c) {
-            Ls[c * NT + th] = tau;
-            Li[c * NT + th] = -1;
+        // Step A (all 16 warps): warp w copies its 32 accumulator lanes
+        // (quarter w & 3) x 16 columns (group w >> 2) of a 64-column chunk
+        // from tensor memory to the transposed tile sT[row][col].
+        // Step B: warp w owns rows 8w .. 8w+7 and scans them 32 columns per
+        // instruction: one compare, a ballot, and the rare candidates go into
+        // the row's list one at a time, all lanes in step.
+        const int quarter = warp & 3, cgroup = warp >> 2;
+        RowList<R> lists[ROWS_PER_WARP];
+        unsigned long long worst[ROWS_PER_WARP];
+#pragma unroll
+        for (int i = 0; i < ROWS_PER_WARP; ++i) {
+            lists[i].init(C, lane);
+            worst[i] = kScoreSentinel;
         }
         const uint32_t trow = tmem + (uint32_t(32 * quarter) << 16);
-        for (int t = 0; t < ntiles; ++t) {
+        constexpr int NCHUNK = kT5Cols / kT5Chunk;
+        if (tid < kT5Rows) sThr[tid] = __int_as_float(0x7f800000);
+        asm volatile("bar.sync 1, %0;" ::"r"(NEPI) : "memory");
+        int step = 0;  // chunk counter over all tiles (selects the sT buffer)
+        bool pending = false;  // step B of the previous chunk still to do
+        int prev_base = 0;
+        auto scan_chunk = [&](int buf, int col_base) {
+            const float* T = sT + buf * kT5Rows * kT5TStride;
+#pragma unroll
+            for (int i = 0; i < ROWS_PER_WARP; ++i) {
+                const int row = warp * ROWS_PER_WARP + i;
+                if (sHit[buf * kT5Rows + row] == 0u) continue;  // no score of this row beat its threshold
+                const float* Tr = T + row * kT5TStride;
+#pragma unroll
+                for (int sl = 0; sl < kT5Chunk; sl += 32) {
+                    const float sc = Tr[sl + lane];
+                    const int ref = col_base + sl + lane;
+                    const float wsc = key_score(worst[i]);
+                    unsigned m = __ballot_sync(0xFFFFFFFFu, sc <= wsc && ref < r1);
+                    while (m) {
+                        const int src = __ffs(m) - 1;
+                        m &= m - 1;
+                        const unsigned long long key =
+                            __shfl_sync(0xFFFFFFFFu, score_key(sc, uint32_t(ref)), src);
+                        if (key < worst[i]) {
+                            lists[i].insert(key, lane);
+                            worst[i] = lists[i].worst();
+                        }
+                    }
+                }
+                if (lane == 0) sThr[row] = key_score(worst[i]);
+            }
+        };
+        bool ok = true;
+        for (int t = 0; t < ntiles && ok; ++t) {
             const int st = t & 1;
             const uint32_t ph = (t >> 1) & 1;
-            int ok = 1;
-            if (lane == 0) ok = sm100::mbar_wait(&mma_done[st], ph, kT5MaxTries) && !abort_sh;
-            ok = __shfl_sync(0xFFFFFFFFu, ok, 0);
-            if (!ok) {
+            int w_ok = 1;
+            if (lane == 0) w_ok = sm100::mbar_wait(&mma_done[st], ph, kT5MaxTries) && !abort_sh;
+            w_ok = __shfl_sync(0xFFFFFFFFu, w_ok, 0);
+            if (!w_ok) {
                 if (lane == 0) {
                     atomicExch(&abort_sh, 1);
                     atomicExch(a.err, 1);
                 }
-                break;
+                ok = false;
             }
-            sm100::tc_fence_after();
-            const int cbase = r0 + t * kT5Cols + half * (kT5Cols / 2);
-#pragma unroll 1
-            for (int c = 0; c < kT5Cols / 2; c += 16) {
-                float v[16];
-                sm100::tmem_ld16(trow + uint32_t(st * kT5Cols + half * (kT5Cols / 2) + c), v);
+            // epilogue warps agree on `ok` through the named barrier below
+            for (int ch = 0; ch < NCHUNK; ++ch) {
+                const int buf = step & 1;
+                if (ok) {
+                    sm100::tc_fence_after();
+                    float v[16];
+                    sm100::tmem_ld16(trow + uint32_t(st * kT5Cols + ch * kT5Chunk + cgroup * 16), v);
+                    const int myrow = 32 * quarter + lane;
+                    float* dst = sT + buf * kT5Rows * kT5TStride + myrow * kT5TStride + cgroup * 16;
 #pragma unroll
-                for (int i = 0; i < 16; ++i) {
-                    const int ref = cbase + c + i;
-                    if (v[i] < tau && ref < r1) {
-                        int pos = cnt < CH ? cnt : CH - 1;
-                        while (pos > 0 && Ls[(pos - 1) * NT + th] > v[i]) {
-                            Ls[pos * NT + th] = Ls[(pos - 1) * NT + th];
-                            Li[pos * NT + th] = Li[(pos - 1) * NT + th];
-                            --pos;
-                        }
-                        Ls[pos * NT + th] = v[i];
-                        Li[pos * NT + th] = ref;
-                        cnt = min(cnt + 1, CH);
-                        if (cnt == CH) tau = Ls[(CH - 1) * NT + th];
+                    for (int i = 0; i < 16; i += 4)
+                        *reinterpret_cast<float4*>(dst + i) = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
+                    // pre-filter against the row's (possibly stale, never too small) threshold
+                    const float thr = sThr[myrow];
+                    bool hit = false;
+#pragma unroll
+                    for (int i = 0; i < 16; ++i) hit |= v[i] <= thr;
+                    reinterpret_cast<uint8_t*>(sHit + buf * kT5Rows + myrow)[cgroup] = hit ? 1 : 0;
+                    if (ch == NCHUNK - 1) {  // this tile's accumulator is no longer read
+                        sm100::tc_fence_before();
+                        __syncwarp();
+                        if (lane == 0) sm100::mbar_arrive(&epi_done[st]);
                     }
                 }
+                // previous chunk's rows while this one lands in the other buffer
+                if (pending) scan_chunk(buf ^ 1, prev_base);
+                asm volatile("bar.sync 1, %0;" ::"r"(NEPI) : "memory");
+                const int bad = abort_sh;
+                if (bad) ok = false;
+                pending = ok;
+                prev_base = r0 + t * kT5Cols + ch * kT5Chunk;
+                ++step;
+                if (!ok) break;
             }
-            sm100::tc_fence_before();
-            __syncwarp();
-            if (lane == 0) sm100::mbar_arrive(&epi_done[st]);
         }
-        // row's candidates: this thread's list is one half of the row's 2*CH
-        const int row = 32 * quarter + lane;
-        const int q = blockIdx.x * kT5Rows + row;
-        if (q < a.nq) {
-            const long long base = ((long long)q * a.nsplit + blockIdx.y) * (2 * CH) + half * CH;
-            for (int c = 0; c < CH; ++c) {
-                a.cand_s[base + c] = Ls[c * NT + th];
-                a.cand_i[base + c] = Li[c * NT + th];
+        if (pending) scan_chunk((step - 1) & 1, prev_base);
+        // write the lists: C candidates per row and the row threshold
+#pragma unroll
+        for (int i = 0; i < ROWS_PER_WARP; ++i) {
+            const int row = warp * ROWS_PER_WARP + i;
+            const int q = blockIdx.x * kT5Rows + row;
+            if (q < a.nq) {
+                const long long base = ((long long)q * a.nsplit + blockIdx.y) * C;
+#pragma unroll
+                for (int r = 0; r < R; ++r) {
+                    const int sidx = r * 32 + lane;
+                    const int o = sidx - (32 * R - C);
+                    if (o >= 0) {
+                        const unsigned long long key = lists[i].slot[r];
+                        const bool real = key != kScoreSentinel;
+                        a.cand_s[base + o] = key_score(key);
+                        a.cand_i[base + o] = real ? int32_t(uint32_t(key)) : -1;
+                    }
+                }
+                if (lane == 0) a.tau[(long long)q * a.nsplit + blockIdx.y] = key_score(worst[i]);
             }
-            Ls[0 * NT + th] = cnt == CH ? tau : __int_as_float(0x7f800000);  // reuse slot 0 for the threshold
         }
     }
     // teardown: everyone done with tensor memory
     sm100::tc_fence_before();
     __syncthreads();
     sm100::tc_fence_after();
-    if (warp < 4) {  // one thread per row writes min(tau of both halves)
-        const int row = 32 * warp + lane;
-        const int q = blockIdx.x * kT5Rows + row;
-        if (q < a.nq) {
-            const float t0 = Ls[0 * NT + tid], t1 = Ls[0 * NT + tid + 128];
-            a.tau[(long long)q * a.nsplit + blockIdx.y] = fminf(t0, t1);
-        }
-    }
     if (warp == kT5EpiWarps) sm100::tmem_dealloc(tmem, 512);
 }
 

@@ -38,6 +38,7 @@ struct KdArgs {
     const PointRec<T>* pts;  // [n] in leaf order
     const T* medians;        // [2^L - 1] heap order
     const int32_t* leaf_off; // [2^L + 1]
+    const PointRec<T>* boxes;// [2 * (2^(L+1) - 1)] node bounding boxes (lo, hi), or null
     int levels;              // L
     int smem_levels;         // S <= L: levels staged in shared memory
     const T* q;              // [nq, D]
@@ -80,7 +81,53 @@ struct TreeView {
     int levels;
     int smem_levels;  // top levels whose split values are in s_med
     const T* s_med;
+    const PointRec<T>* boxes;  // node bounding boxes, or null
 };
+
+// Lower bound on the computed distance from q to any point inside the
+// bounding box of `node`: per axis the gap to the box, rounded and squared
+// as sqdist does, summed in the same order.  By monotonicity of rounding it
+// never exceeds sqdist(q, p) for a point p in the box; an empty box
+// (lo = +inf, hi = -inf) gives +inf.
+template <typename T, int D>
+__device__ __forceinline__ T box_bound(const PointRec<T>* boxes, int node, const T (&q)[D]) {
+    const PointRec<T> lo = load_rec(boxes + 2 * node);
+    const PointRec<T> hi = load_rec(boxes + 2 * node + 1);
+    const T l[3] = {lo.x, lo.y, lo.z};
+    const T h[3] = {hi.x, hi.y, hi.z};
+    T e[D];
+#pragma unroll
+    for (int c = 0; c < D; ++c) {
+        const T g = q[c] < l[c] ? sub_rn(q[c], l[c]) : (q[c] > h[c] ? sub_rn(q[c], h[c]) : T(0));
+        e[c] = mul_rn(g, g);
+    }
+    T b = e[0];
+    if (D > 1) b = add_rn(b, e[1]);
+    if (D > 2) b = add_rn(b, e[2]);
+    return b;
+}
+
+// Sort R keys ascending in registers (bitonic network, R a power of two).
+template <typename T, int R>
+__device__ __forceinline__ void bitonic_sort(Key<T> (&v)[R]) {
+#pragma unroll
+    for (int size = 2; size <= R; size <<= 1) {
+#pragma unroll
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+#pragma unroll
+            for (int i = 0; i < R; ++i) {
+                const int j = i ^ stride;
+                if (j > i) {
+                    const bool up = (i & size) == 0;
+                    const bool sw = up ? v[j].lt(v[i]) : v[i].lt(v[j]);
+                    const Key<T> a = v[i], b = v[j];
+                    v[i] = sw ? b : a;
+                    v[j] = sw ? a : b;
+                }
+            }
+        }
+    }
+}
 
 // Exhaustive-equivalent KNN for one query, served by a group of G lanes;
 // writes k results to out_d[0..k) / out_i[0..k).
@@ -95,6 +142,7 @@ __device__ __forceinline__ void kd_search(const TreeView<T>& tv, const T (&q)[D]
     StackEntry<T, D> stk[kMaxLevels];
     int sp = 0;
     int node = 0, depth = 0;
+    bool home = true;  // the first leaf reached is the query's own cell
     T e[D];
 #pragma unroll
     for (int c = 0; c < D; ++c) e[c] = T(0);
@@ -119,27 +167,61 @@ __device__ __forceinline__ void kd_search(const TreeView<T>& tv, const T (&q)[D]
             ++depth;
             ax = (ax + 1 == D) ? 0 : ax + 1;
         }
-        // scan the leaf bucket, G points at a time
-        {
+        // scan the leaf bucket, G points at a time (unless its box is out of reach)
+        if (!tv.boxes || box_bound<T, D>(tv.boxes, node, q) <= worst_d) {
             const int leaf = node - first_leaf;
-            const int beg = __ldg(tv.leaf_off + leaf);
+            int beg = __ldg(tv.leaf_off + leaf);
             const int end = __ldg(tv.leaf_off + leaf + 1);
-            for (int j0 = beg; j0 < end; j0 += G) {
-                const int j = j0 + gl;
-                Key<T> mine = Key<T>::sentinel();
+            if (G == 1 && home && k == R && end - beg >= R) {
+                // fill the whole list from the home cell with one sorting
+                // network instead of R single insertions
+                Key<T> v[R];
+#pragma unroll
+                for (int i = 0; i < R; ++i) {
+                    const PointRec<T> p = load_rec(tv.pts + beg + i);
+                    v[i] = Key<T>::make(sqdist<T, D>(q, p), rec_index(p));
+                }
+                bitonic_sort<T, R>(v);
+#pragma unroll
+                for (int i = 0; i < R; ++i) list.slot[i] = v[i];
+                worst = list.worst(gmask);
+                beg += R;
+            }
+            if constexpr (G == 1) {
+                // two records per step: independent loads and distance chains
+                int j = beg;
+                for (; j + 1 < end; j += 2) {
+                    const PointRec<T> p0 = load_rec(tv.pts + j);
+                    const PointRec<T> p1 = load_rec(tv.pts + j + 1);
+                    const Key<T> k0 = Key<T>::make(sqdist<T, D>(q, p0), rec_index(p0));
+                    const Key<T> k1 = Key<T>::make(sqdist<T, D>(q, p1), rec_index(p1));
+                    worst = offer<T, G, R>(list, k0, worst, gmask, gl, gbase);
+                    worst = offer<T, G, R>(list, k1, worst, gmask, gl, gbase);
+                }
                 if (j < end) {
                     const PointRec<T> p = load_rec(tv.pts + j);
-                    mine = Key<T>::make(sqdist<T, D>(q, p), rec_index(p));
+                    worst = offer<T, G, R>(list, Key<T>::make(sqdist<T, D>(q, p), rec_index(p)), worst, gmask, gl,
+                                           gbase);
                 }
-                worst = offer<T, G, R>(list, mine, worst, gmask, gl, gbase);
+            } else {
+                for (int j0 = beg; j0 < end; j0 += G) {
+                    const int j = j0 + gl;
+                    Key<T> mine = Key<T>::sentinel();
+                    if (j < end) {
+                        const PointRec<T> p = load_rec(tv.pts + j);
+                        mine = Key<T>::make(sqdist<T, D>(q, p), rec_index(p));
+                    }
+                    worst = offer<T, G, R>(list, mine, worst, gmask, gl, gbase);
+                }
             }
             worst_d = worst.dist();
         }
+        home = false;
         // resume at the deepest stacked cell that can still hold a neighbour
         bool resumed = false;
         while (sp > 0) {
             const StackEntry<T, D> s = stk[--sp];
-            if (cell_bound<T, D>(s.e) <= worst_d) {
+            if (cell_bound<T, D>(s.e) <= worst_d && (!tv.boxes || box_bound<T, D>(tv.boxes, s.node, q) <= worst_d)) {
                 node = s.node;
 #pragma unroll
                 for (int c = 0; c < D; ++c) e[c] = s.e[c];
@@ -159,7 +241,7 @@ __device__ __forceinline__ void kd_query_one(const KdArgs<T>& a, const T* s_med,
     T q[D];
 #pragma unroll
     for (int c = 0; c < D; ++c) q[c] = a.q[(long long)qi * D + c];
-    const TreeView<T> tv{a.pts, a.medians, a.leaf_off, a.levels, a.smem_levels, s_med};
+    const TreeView<T> tv{a.pts, a.medians, a.leaf_off, a.levels, a.smem_levels, s_med, a.boxes};
     kd_search<T, D, G, R>(tv, q, a.k, a.out_d + (long long)qi * a.k, a.out_i + (long long)qi * a.k, gmask, gl,
                           gbase);
 }
@@ -216,7 +298,6 @@ __global__ void k_bin_count(const T* __restrict__ q, int nq, const T* __restrict
     pos_of[i] = atomicAdd(counts + bin, 1);
 }
 
-__global__ void k_bin_scan(int* counts, int nbins, int* work);
 __global__ void k_bin_scatter(int nq, const int* bin_of, const int* pos_of, const int* offsets, int* order);
 
 // Per-(T, D) launcher implemented in kd_query_<type>_d<D>.cu.

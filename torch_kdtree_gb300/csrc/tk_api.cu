@@ -7,6 +7,7 @@
 #include <vector>
 
 #include "kd_query.cuh"
+#include "sort.cuh"
 #include "tk_internal.h"
 
 namespace tk {
@@ -52,43 +53,6 @@ void clear_error() { g_err.clear(); }
 
 // ------------------------------------------------------------ binning --
 
-__global__ void k_bin_scan(int* counts, int nbins, int* work) {
-    // One block of 1024 threads: exclusive scan of counts[0..nbins) in place.
-    __shared__ int warp_sums[32];
-    const int tid = threadIdx.x;
-    const int per = (nbins + blockDim.x - 1) / blockDim.x;
-    const int beg = min(nbins, tid * per), end = min(nbins, beg + per);
-    int sum = 0;
-    for (int i = beg; i < end; ++i) sum += counts[i];
-    // inclusive scan of per-thread sums
-    const int lane = tid & 31, wid = tid >> 5;
-    int v = sum;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const int t = __shfl_up_sync(0xFFFFFFFFu, v, o);
-        if (lane >= o) v += t;
-    }
-    if (lane == 31) warp_sums[wid] = v;
-    __syncthreads();
-    if (wid == 0) {
-        int w = lane < (int)(blockDim.x >> 5) ? warp_sums[lane] : 0;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const int t = __shfl_up_sync(0xFFFFFFFFu, w, o);
-            if (lane >= o) w += t;
-        }
-        warp_sums[lane] = w;
-    }
-    __syncthreads();
-    int run = v - sum + (wid > 0 ? warp_sums[wid - 1] : 0);
-    for (int i = beg; i < end; ++i) {
-        const int c = counts[i];
-        counts[i] = run;
-        run += c;
-    }
-    if (tid == 0) *work = 0;
-}
-
 __global__ void k_bin_scatter(int nq, const int* bin_of, const int* pos_of, const int* offsets, int* order) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nq) return;
@@ -106,7 +70,7 @@ int bin_levels(int L, int64_t nq) {
 }
 
 struct WsLayout {
-    size_t counter = 0, counts = 0, bin_of = 0, pos_of = 0, order = 0, total = 0;
+    size_t counter = 0, counts = 0, bin_of = 0, pos_of = 0, order = 0, scan = 0, total = 0;
 };
 
 WsLayout ws_layout(int L, int64_t nq) {
@@ -123,6 +87,8 @@ WsLayout ws_layout(int L, int64_t nq) {
     o += align_up(sizeof(int) * size_t(nq), 256);
     w.order = o;
     o += align_up(sizeof(int) * size_t(nq), 256);
+    w.scan = o;
+    o += scan_workspace_bytes(int64_t(1) << B);
     w.total = o;
     return w;
 }
@@ -199,9 +165,11 @@ int run_query(const tk_tree* t, const T* q, int nq, int k, T* dists, int32_t* id
         int* pos_of = reinterpret_cast<int*>(ws + w.pos_of);
         int* ord = reinterpret_cast<int*>(ws + w.order);
         e = cudaMemsetAsync(counts, 0, sizeof(int) * nbins, s);
+        if (e == cudaSuccess) e = cudaMemsetAsync(counter, 0, sizeof(int), s);
         if (e != cudaSuccess) return fail(TK_ECUDA, std::string("memset: ") + cudaGetErrorString(e));
         bin_count_launch<T, D>(q, nq, static_cast<const T*>(t->d_medians), B, counts, bin_of, pos_of, s);
-        k_bin_scan<<<1, 1024, 0, s>>>(counts, nbins, counter);
+        e = exclusive_scan(counts, nbins, ws + w.scan, s);
+        if (e != cudaSuccess) return fail(TK_ECUDA, std::string("bin scan: ") + cudaGetErrorString(e));
         k_bin_scatter<<<(nq + 255) / 256, 256, 0, s>>>(nq, bin_of, pos_of, counts, ord);
         e = cudaGetLastError();
         if (e != cudaSuccess) return fail(TK_ECUDA, std::string("binning launch: ") + cudaGetErrorString(e));
@@ -215,6 +183,7 @@ int run_query(const tk_tree* t, const T* q, int nq, int k, T* dists, int32_t* id
     a.pts = static_cast<const PointRec<T>*>(t->d_pts);
     a.medians = static_cast<const T*>(t->d_medians);
     a.leaf_off = t->d_leaf_off;
+    a.boxes = o.prune_boxes == 0 ? nullptr : static_cast<const PointRec<T>*>(t->d_boxes);
     a.levels = L;
     a.smem_levels = S;
     a.q = q;
@@ -252,15 +221,24 @@ int upload_tree(tk_tree* t, const HostTree<T>& h) {
     const size_t b_pts = sizeof(PointRec<T>) * size_t(n);
     const size_t b_med = sizeof(T) * h.medians.size();
     const size_t b_off = sizeof(int32_t) * h.leaf_off.size();
+    const size_t nnodes = h.box_lo.size() / 3;
+    std::vector<PointRec<T>> boxes(2 * nnodes);
+    for (size_t i = 0; i < nnodes; ++i) {
+        boxes[2 * i] = PointRec<T>{h.box_lo[3 * i], h.box_lo[3 * i + 1], h.box_lo[3 * i + 2], T(0)};
+        boxes[2 * i + 1] = PointRec<T>{h.box_hi[3 * i], h.box_hi[3 * i + 1], h.box_hi[3 * i + 2], T(0)};
+    }
+    const size_t b_box = sizeof(PointRec<T>) * boxes.size();
     cudaError_t e = cudaMalloc(&t->d_pts, b_pts);
     if (e == cudaSuccess) e = cudaMalloc(&t->d_medians, std::max<size_t>(b_med, sizeof(T)));
     if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&t->d_leaf_off), b_off);
+    if (e == cudaSuccess) e = cudaMalloc(&t->d_boxes, b_box);
     if (e != cudaSuccess) return fail(TK_ENOMEM, std::string("device allocation: ") + cudaGetErrorString(e));
     e = cudaMemcpy(t->d_pts, recs.data(), b_pts, cudaMemcpyHostToDevice);
     if (e == cudaSuccess && b_med) e = cudaMemcpy(t->d_medians, h.medians.data(), b_med, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(t->d_leaf_off, h.leaf_off.data(), b_off, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(t->d_boxes, boxes.data(), b_box, cudaMemcpyHostToDevice);
     if (e != cudaSuccess) return fail(TK_ECUDA, std::string("tree upload: ") + cudaGetErrorString(e));
-    t->device_bytes = int64_t(b_pts + b_med + b_off);
+    t->device_bytes = int64_t(b_pts + b_med + b_off + b_box);
     return TK_OK;
 }
 
@@ -268,7 +246,8 @@ void free_tree_device(tk_tree* t) {
     if (t->d_pts) cudaFree(t->d_pts);
     if (t->d_medians) cudaFree(t->d_medians);
     if (t->d_leaf_off) cudaFree(t->d_leaf_off);
-    t->d_pts = t->d_medians = nullptr;
+    if (t->d_boxes) cudaFree(t->d_boxes);
+    t->d_pts = t->d_medians = t->d_boxes = nullptr;
     t->d_leaf_off = nullptr;
 }
 
@@ -410,7 +389,7 @@ int tk_tree_query(const tk_tree* t, const void* q, int64_t nq, int k, void* dist
     const size_t need = ws_layout(t->levels, nq).total;
     if (!workspace || workspace_bytes < need)
         return fail(TK_EWORKSPACE, "workspace too small: need " + std::to_string(need) + " bytes");
-    tk_query_opts o{0, -1, -1, 0, 0, nullptr, nullptr};
+    tk_query_opts o{0, -1, -1, 0, 0, nullptr, nullptr, -1};
     if (opts) o = *opts;
     DeviceGuard g(t->device);
     cudaStream_t s = static_cast<cudaStream_t>(stream);
@@ -441,14 +420,14 @@ int tk_tree_query(const tk_tree* t, const void* q, int64_t nq, int k, void* dist
 //
 // Scratch of tk_tree_query_noalloc: one static device array, sized for
 // TK_NOALLOC_MAX_QUERIES queries (counter + 2^16 cell counts + three int32
-// arrays of that many queries, laid out as ws_layout() lays out a caller's
-// workspace).  Every GPU that loads the library holds it until the process
+// arrays of that many queries + the cell-count scan's tile sums, laid out as
+// ws_layout() lays out a caller's workspace).  Every GPU that loads the library holds it until the process
 // exits, and every call on a device shares it.
 namespace tk {
 namespace {
 
 constexpr size_t kNoAllocScratchBytes =
-    256 + sizeof(int) * (size_t(1) << kMaxBinLevels) + 3 * sizeof(int) * size_t(TK_NOALLOC_MAX_QUERIES);
+    256 + sizeof(int) * (size_t(1) << kMaxBinLevels) + 3 * sizeof(int) * size_t(TK_NOALLOC_MAX_QUERIES) + 256;
 static_assert(TK_NOALLOC_MAX_QUERIES % 64 == 0, "each scratch array must stay 256-byte aligned");
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
@@ -495,7 +474,7 @@ extern "C" int tk_tree_query_noalloc(const tk_tree* t, const void* q, int64_t nq
     if (rc != TK_OK) return rc;
     if (ws_layout(t->levels, nq).total > kNoAllocScratchBytes)
         return fail(TK_EINVAL, "query needs more scratch than the static array holds");
-    tk_query_opts o{0, -1, -1, 0, 0, nullptr, nullptr};
+    tk_query_opts o{0, -1, -1, 0, 0, nullptr, nullptr, -1};
     if (opts) o = *opts;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     char* ws = static_cast<char*>(scratch);

@@ -29,6 +29,10 @@ struct HostTree {
     std::vector<int32_t> perm;        // [n] original index of structured point i
     std::vector<T> medians;           // [2^L - 1] heap order; axis = depth % dims
     std::vector<int32_t> leaf_off;    // [2^L + 1] prefix offsets of the leaves
+    // Tight bounding boxes of every node's points, heap order over all
+    // 2^(L+1) - 1 nodes (leaves last), 3 coordinates each (unused ones 0);
+    // empty nodes have lo = +inf, hi = -inf.
+    std::vector<T> box_lo, box_hi;
 };
 
 // Builds the tree (tree_build.cpp).  Returns TK_OK or sets the error.
@@ -51,5 +55,6 @@ struct tk_tree {
     void* d_pts = nullptr;       // point records: coordinates + original index (see tk_device.cuh)
     void* d_medians = nullptr;   // T[2^L - 1]
     int32_t* d_leaf_off = nullptr;  // int32[2^L + 1]
+    void* d_boxes = nullptr;     // per node {lo.xyz, 0}, {hi.xyz, 0} (see tk_device.cuh)
     int64_t device_bytes = 0;
 };

@@ -19,6 +19,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cmath>
+#include <limits>
 #include <thread>
 
 #include "tk_internal.h"
@@ -137,6 +138,27 @@ int build_host_tree(const T* pts, int64_t n, int dims, int levels, int n_threads
         for (int c = 0; c < dims; ++c) out.structured[i * dims + c] = recs[i].c[c];
         out.perm[i] = recs[i].orig;
     }
+    // bounding boxes: leaves from their points, inner nodes from their children
+    const int64_t nleaves = int64_t(1) << levels;
+    const int64_t nnodes = 2 * nleaves - 1;
+    const T inf = std::numeric_limits<T>::infinity();
+    out.box_lo.assign(static_cast<size_t>(nnodes) * 3, inf);
+    out.box_hi.assign(static_cast<size_t>(nnodes) * 3, -inf);
+    for (int64_t l = 0; l < nleaves; ++l) {
+        const int64_t node = nleaves - 1 + l;
+        T* lo = &out.box_lo[node * 3];
+        T* hi = &out.box_hi[node * 3];
+        for (int32_t i = out.leaf_off[l]; i < out.leaf_off[l + 1]; ++i)
+            for (int c = 0; c < 3; ++c) {
+                lo[c] = std::min(lo[c], recs[i].c[c]);
+                hi[c] = std::max(hi[c], recs[i].c[c]);
+            }
+    }
+    for (int64_t node = nleaves - 2; node >= 0; --node)
+        for (int c = 0; c < 3; ++c) {
+            out.box_lo[node * 3 + c] = std::min(out.box_lo[(2 * node + 1) * 3 + c], out.box_lo[(2 * node + 2) * 3 + c]);
+            out.box_hi[node * 3 + c] = std::max(out.box_hi[(2 * node + 1) * 3 + c], out.box_hi[(2 * node + 2) * 3 + c]);
+        }
     return TK_OK;
 }
 
