@@ -530,6 +530,58 @@ def run_brute(args):
 
 
 
+def run_plain(args):
+    """Plain KD-tree KNN: 100,000 refs and 10,000 queries N(0,1)*1e3, k=5, the
+    reference's default depth; GPU query (graph-replayed, inputs resident) vs
+    the reference CPU query (oracle restatement) on the same inputs, checked
+    for exactness."""
+    import torch
+
+    import torch_kdtree_gb300 as tk
+    from torch_kdtree_gb300.nn_distance import knn_query_raw
+    from torch_kdtree_gb300.synthetic import plain_cloud
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    ref_np, q_np = plain_cloud()
+    ref = torch.from_numpy(ref_np).to(dev)
+    q = torch.from_numpy(q_np).to(dev)
+    k = 5
+    tree = tk.build_kd_tree(ref)
+    d = torch.empty(len(q), k, device=dev)
+    i = torch.empty(len(q), k, dtype=torch.int32, device=dev)
+    s = torch.cuda.Stream(dev)
+    s.wait_stream(torch.cuda.current_stream(dev))
+    with torch.cuda.stream(s):
+        knn_query_raw(tree._tree, q, k, d, i)
+    torch.cuda.current_stream(dev).wait_stream(s)
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        knn_query_raw(tree._tree, q, k, d, i)
+    ms = _event_ms(g.replay, max(args.steps, 20), args.warmup)
+    t = sum(ms) / len(ms) / 1e3
+    g.replay()
+    torch.cuda.synchronize()
+    from oracle import oracle as O
+    O.build()
+    threads = os.cpu_count() or 1
+    lay = O.build_tree(ref_np, O.default_levels(len(ref_np)), nthreads=threads)
+    t0 = time.perf_counter()
+    od, oi = O.query_tree(lay, q_np, k, nthreads=threads)
+    cpu_t = time.perf_counter() - t0
+    cmp = O.compare_knn(od, oi, d.cpu().numpy(), i.cpu().numpy())
+    line = {
+        "metric": "KNN queries/s, plain KD-tree (100,000 refs, 10,000 queries N(0,1)*1e3, d=3, k=5)",
+        "value": len(q) / t, "unit": UNIT, "n_gpus": 1, "steps": len(ms), "warmup": args.warmup,
+        "ms_per_step": 1e3 * t, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded numpy)", "config": {"workload": "plain KD query, levels 13", "graph_captured": True},
+        "cpu_baseline": {"value": len(q) / cpu_t, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": "all 10,000 queries"},
+        "exactness_vs_reference_cpu": {"index_mismatches_non_tie": cmp.mismatches, "tie_queries": cmp.tie_queries,
+                                       "dist_bit_mismatches": cmp.dist_bit_mismatch},
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_brute_tc(args):
     """Tensor-core brute force vs the FP32 CUDA-core brute force: 262,144 refs,
     65,536 queries, N(0,1) in d = 8 and 32 with 5% exact duplicate refs, k=32.
@@ -599,7 +651,7 @@ def main():
     p.add_argument("--tpq", type=int, default=0, help="chosen lanes per query (skips the autotuner with --levels)")
     p.add_argument("--boxes", type=int, default=1, help="chosen: prune with node bounding boxes (with --levels/--tpq)")
     p.add_argument("--profile", action="store_true", help="run one chosen and one plain query only (for ncu)")
-    p.add_argument("--workload", default="kd", choices=["kd", "batched", "backward", "brute", "brute_tc"],
+    p.add_argument("--workload", default="kd", choices=["kd", "plain", "batched", "backward", "brute", "brute_tc"],
                    help="kd (default): the headline large single-cloud query; the others measure the "
                         "batched, backward and brute-force paths")
     p.add_argument("--leaf-size", type=int, default=16, help="target points per leaf of tuned batch trees")
@@ -613,7 +665,7 @@ def main():
         return
     if args.workload != "kd":
         if rank == 0:
-            {"batched": run_batched, "backward": run_backward, "brute": run_brute,
+            {"plain": run_plain, "batched": run_batched, "backward": run_backward, "brute": run_brute,
              "brute_tc": run_brute_tc}[args.workload](args)
         return
     if world > 1:
