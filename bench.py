@@ -109,6 +109,26 @@ def measured_peak_hbm():
         return 6800.0, "fallback"
 
 
+def fp64_error(ref, q, dists, idx, chunk=1 << 18):
+    """Max relative error of the returned FP32 squared distances against the
+    same (query, neighbour) pairs recomputed in FP64 from the FP32 inputs, and
+    the number of queries with an exact distance tie inside their returned
+    list (ties are ordered by lower original index)."""
+    import torch
+    worst = 0.0
+    ties = 0
+    for a in range(0, q.shape[0], chunk):
+        qq = q[a:a + chunk].double()
+        ii = idx[a:a + chunk].long()
+        d64 = ((ref[ii].double() - qq[:, None, :]) ** 2).sum(-1)
+        dd = dists[a:a + chunk].double()
+        rel = (dd - d64).abs() / d64.clamp_min(torch.finfo(torch.float64).tiny)
+        rel = torch.where(d64 > 0, rel, (dd - d64).abs())
+        worst = max(worst, float(rel.max()))
+        ties += int((dists[a:a + chunk, 1:] == dists[a:a + chunk, :-1]).any(1).sum())
+    return {"max_rel_err": worst, "queries_with_equal_distances_in_list": ties}
+
+
 def profiled_traffic(kernel_tag: str):
     """DRAM bytes per launch of a kernel from its committed ncu summary
     (profiles/<kernel_tag>.md, line 'traffic_bytes_per_launch: <int>'), or None."""
@@ -209,7 +229,7 @@ def run_ours(args, rank, world):
     if args.levels and args.tpq:
         from torch_kdtree_gb300.autotune import Choice
         ch = Choice(levels=args.levels, threads_per_query=args.tpq, ms=float("nan"), plain_levels=plain.levels,
-                    table=[], prune_boxes=args.boxes)
+                    table=[], prune_boxes=args.boxes, traversal=args.traversal)
     else:
         ch = autotune(ref, q, K_NN, use_cache=False)
     tune_s = time.perf_counter() - t0
@@ -284,7 +304,7 @@ def run_ours(args, rank, world):
     ke.record()  # materialise the events
     torch.cuda.synchronize()
     kopts = QueryOpts.make(threads_per_query=ch.threads_per_query, kernel_start_event=ks.cuda_event,
-                           kernel_stop_event=ke.cuda_event, prune_boxes=ch.prune_boxes)
+                           kernel_stop_event=ke.cuda_event, prune_boxes=ch.prune_boxes, traversal=ch.traversal)
     kern_ms = []
     for _ in range(max(3, args.steps)):
         flush.zero_()
@@ -324,7 +344,9 @@ def run_ours(args, rank, world):
     peak, peak_kind = measured_peak_hbm()
     alg = algorithmic_bytes(n_ref, nq, K_NN, ch.levels)
     achieved = alg / (kern_avg / 1e3) / 1e9
-    traffic = profiled_traffic("kd_query_cube_sphere_4M_k16")
+    kernel_name = "k_kd_packet" if ch.traversal == 2 else "k_kd_query"
+    traffic = profiled_traffic(kernel_name[2:] + "_cube_sphere_4M_k16")
+    fp64 = fp64_error(ref, q, d_ch, i_ch)
 
     # ---- CPU baseline (oracle / reference CPU path) on a bounded sample, plus an exactness check of that sample
     cpu = None
@@ -339,7 +361,7 @@ def run_ours(args, rank, world):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded numpy, shapes and distributions of the workload)",
         "config": {"workload": WORKLOAD, "levels": ch.levels, "threads_per_query": ch.threads_per_query,
-                   "prune_boxes": ch.prune_boxes,
+                   "prune_boxes": ch.prune_boxes, "traversal": {1: "per-query stacks", 2: "warp packets"}[ch.traversal],
                    "graph_captured": True, "l2": f"flushed between steps ({L2_FLUSH_BYTES >> 20} MiB write)",
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                    "tree_build_s": {"plain": build_plain_s, "chosen": build_chosen_s}, "autotune_s": tune_s},
@@ -349,10 +371,11 @@ def run_ours(args, rank, world):
         "identical_results_plain_vs_chosen": same,
         "autotune_table": [list(map(lambda x: round(x, 4) if isinstance(x, float) else x, r)) for r in ch.table],
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_kind": peak_kind, "traffic": traffic, "kernel": "k_kd_query",
+                     "peak_kind": peak_kind, "traffic": traffic, "kernel": kernel_name,
                      "kernel_ms": kern_avg, "algorithmic_bytes_per_launch": alg},
         "cpu_baseline": cpu,
         "exactness_vs_oracle_sample": exact,
+        "fp32_dists_vs_fp64_recomputation": fp64,
         "e2e": {"value": world * nq * args.steps / (t_e2e / 1e3), "unit": UNIT,
                 "h2d_bytes_per_step": q_host.numel() * 4,
                 "d2h_bytes_per_step": d_host.numel() * 4 + i_host.numel() * 4,
@@ -650,6 +673,8 @@ def main():
     p.add_argument("--levels", type=int, default=0, help="chosen tree depth (skips the autotuner with --tpq)")
     p.add_argument("--tpq", type=int, default=0, help="chosen lanes per query (skips the autotuner with --levels)")
     p.add_argument("--boxes", type=int, default=1, help="chosen: prune with node bounding boxes (with --levels/--tpq)")
+    p.add_argument("--traversal", type=int, default=1, choices=[1, 2],
+                   help="chosen: 1 = per-query stacks, 2 = warp packets (with --levels/--tpq)")
     p.add_argument("--profile", action="store_true", help="run one chosen and one plain query only (for ncu)")
     p.add_argument("--workload", default="kd", choices=["kd", "plain", "batched", "backward", "brute", "brute_tc"],
                    help="kd (default): the headline large single-cloud query; the others measure the "

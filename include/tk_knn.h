@@ -97,6 +97,10 @@ typedef struct tk_query_opts {
     void* kernel_start_event;  /* optional cudaEvent_t recorded right before the KD kernel */
     void* kernel_stop_event;   /* optional cudaEvent_t recorded right after it */
     int32_t prune_boxes;       /* -1 = auto (on), 0 = split planes only, 1 = also node bounding boxes */
+    int32_t traversal;         /* 0 = auto (per-query), 1 = per-query stacks (G lanes per query),
+                                  2 = warp packets: the 32 queries of a warp walk the tree together,
+                                  one lane each, pruning with node boxes (k <= 16; larger k falls
+                                  back to 1; threads_per_query and prune_boxes are then ignored) */
 } tk_query_opts;
 
 /* Bytes of device scratch tk_tree_query needs for nq queries. */

@@ -66,10 +66,41 @@ def test_any_tree_depth_gives_identical_results(levels, oracle):
     q = (rng.random((2500, 3)) * 1.2 - 0.1).astype(np.float32)
     bd, bi = oracle.brute(ref, q, 16)
     for smem in (0, 5, 12):
-        for boxes in (0, 1):
-            d, i = gpu_query(ref, q, 16, levels=levels, smem_levels=smem, prune_boxes=boxes)
+        for boxes, trav in ((0, 1), (1, 1), (1, 2)):
+            d, i = gpu_query(ref, q, 16, levels=levels, smem_levels=smem, prune_boxes=boxes, traversal=trav)
             np.testing.assert_array_equal(d, bd)
             np.testing.assert_array_equal(i, bi)
+
+
+@pytest.mark.parametrize("k", [1, 2, 3, 5, 8, 13, 16, 17, 64])
+@pytest.mark.parametrize("levels", [4, 9, 12])
+def test_warp_packets_give_identical_results(k, levels, oracle):
+    """Warp-packet traversal (one lane per query, the warp walks the tree
+    together): exact for every k it serves, query counts that leave warps
+    partly empty, unbinned order, and k > 16 (falls back to per-query)."""
+    rng = np.random.default_rng(16)
+    ref = rng.standard_normal((30000, 3)).astype(np.float32)
+    q = (rng.standard_normal((3001, 3)) * 1.3).astype(np.float32)
+    bd, bi = oracle.brute(ref, q, k)
+    for binq in (0, 1):
+        d, i = gpu_query(ref, q, k, levels=levels, traversal=2, bin_queries=binq)
+        np.testing.assert_array_equal(d, bd)
+        np.testing.assert_array_equal(i, bi)
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+@pytest.mark.parametrize("d", [1, 2, 3])
+def test_warp_packets_all_instantiations(dtype, d, oracle):
+    rng = np.random.default_rng(17 + d)
+    ref = (rng.standard_normal((5000, d)) * 1e3).astype(dtype)
+    q = (rng.standard_normal((777, d)) * 1e3).astype(dtype)
+    # a cloud with heavy exact duplicates (ties across leaves)
+    ref[2500:] = ref[:2500]
+    for k in (1, 4, 16):
+        bd, bi = oracle.brute(ref, q, k)
+        d_, i_ = gpu_query(ref, q, k, levels=8, traversal=2)
+        np.testing.assert_array_equal(d_, bd)
+        np.testing.assert_array_equal(i_, bi)
 
 
 @pytest.mark.parametrize("dtype", [np.float32, np.float64])
@@ -122,6 +153,10 @@ def test_api_errors():
         t.build_kd_tree(np.random.uniform(size=(10, 436)), device="cuda")  # uncompiled dimension
     with pytest.raises(Exception):
         t.build_kd_tree(torch.randn(10, 3), device="cpu")  # this engine builds CUDA trees only
+    from torch_kdtree_gb300._lib import QueryOpts
+    bad = t.build_kd_tree(pts, query_opts=QueryOpts.make(traversal=3))
+    with pytest.raises(Exception):
+        bad.query(torch.randn(5, 3, device=cuda))  # unknown traversal
 
 
 def test_empty_query_and_result_buffers(oracle):

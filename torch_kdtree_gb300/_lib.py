@@ -49,13 +49,14 @@ class QueryOpts(ctypes.Structure):
     _fields_ = [("threads_per_query", ctypes.c_int32), ("bin_queries", ctypes.c_int32),
                 ("smem_levels", ctypes.c_int32), ("block_threads", ctypes.c_int32),
                 ("blocks_per_sm", ctypes.c_int32), ("kernel_start_event", ctypes.c_void_p),
-                ("kernel_stop_event", ctypes.c_void_p), ("prune_boxes", ctypes.c_int32)]
+                ("kernel_stop_event", ctypes.c_void_p), ("prune_boxes", ctypes.c_int32),
+                ("traversal", ctypes.c_int32)]
 
     @classmethod
     def make(cls, threads_per_query=0, bin_queries=-1, smem_levels=-1, block_threads=0, blocks_per_sm=0,
-             kernel_start_event=None, kernel_stop_event=None, prune_boxes=-1):
+             kernel_start_event=None, kernel_stop_event=None, prune_boxes=-1, traversal=0):
         return cls(threads_per_query, bin_queries, smem_levels, block_threads, blocks_per_sm,
-                   kernel_start_event, kernel_stop_event, prune_boxes)
+                   kernel_start_event, kernel_stop_event, prune_boxes, traversal)
 
 
 _vp = ctypes.c_void_p

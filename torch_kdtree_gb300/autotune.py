@@ -1,4 +1,5 @@
-"""Autotuner for the KD query launch: tree depth (leaf size) and lanes per query.
+"""Autotuner for the KD query launch: tree depth (leaf size), traversal
+(per-query stacks or warp packets), lanes per query and node-box pruning.
 
 For a given reference cloud, a query sample and k, it builds the tree at a
 few depths around the reference's heuristic, times every lanes-per-query
@@ -31,16 +32,18 @@ class Choice:
     threads_per_query: int
     ms: float
     plain_levels: int
-    table: list  # (levels, lanes, boxes, ms) of every timed candidate
+    table: list  # (levels, lanes, boxes, traversal, ms) of every timed candidate
     prune_boxes: int = 1
+    traversal: int = 1  # 1 = per-query stacks, 2 = warp packets
 
     def opts(self) -> QueryOpts:
-        return QueryOpts.make(threads_per_query=self.threads_per_query, prune_boxes=self.prune_boxes)
+        return QueryOpts.make(threads_per_query=self.threads_per_query, prune_boxes=self.prune_boxes,
+                              traversal=self.traversal)
 
 
 def _key(n, nq, k, d, dtype, device) -> str:
     name = torch.cuda.get_device_name(device)
-    return f"{name}|n={n}|q~2^{int(round(math.log2(max(nq, 1))))}|k={k}|d={d}|{dtype}"
+    return f"v2|{name}|n={n}|q~2^{int(round(math.log2(max(nq, 1))))}|k={k}|d={d}|{dtype}"
 
 
 def _load_cache() -> dict:
@@ -81,8 +84,9 @@ def time_query(tree: TorchKDTree, q: torch.Tensor, k: int, opts: QueryOpts, reps
 def autotune(points_ref: torch.Tensor, queries: torch.Tensor, k: int,
              levels_candidates: Optional[Sequence[int]] = None, lanes: Sequence[int] = LANES,
              reps: int = 3, use_cache: bool = True, max_queries: int = 1 << 20) -> Choice:
-    """Pick (levels, threads_per_query) for querying ``points_ref`` with
-    queries like ``queries`` (a sample of at most ``max_queries`` is timed)."""
+    """Pick (levels, traversal, threads_per_query, prune_boxes) for querying
+    ``points_ref`` with queries like ``queries`` (a sample of at most
+    ``max_queries`` is timed)."""
     n, d = points_ref.shape
     key = _key(n, queries.shape[0], k, d, str(points_ref.dtype), points_ref.device)
     cache = _load_cache() if use_cache else {}
@@ -101,17 +105,17 @@ def autotune(points_ref: torch.Tensor, queries: torch.Tensor, k: int,
             tree = build_kd_tree(points_ref, levels=L)
         except Exception:  # too deep for this cloud
             continue
-        for g in lanes:
-            if g * 16 < k:  # a lane holds at most 16 list entries
-                continue
-            for boxes in (1, 0):
-                ms = time_query(tree, q, k, QueryOpts.make(threads_per_query=g, prune_boxes=boxes), reps)
-                table.append((L, g, boxes, ms))
-                if best is None or ms < best[3]:
-                    best = (L, g, boxes, ms)
+        cands = [(g, boxes, 1) for g in lanes if g * 16 >= k for boxes in (1, 0)]  # a lane holds <= 16 keys
+        if k <= 16:
+            cands.append((1, 1, 2))  # warp packets
+        for g, boxes, trav in cands:
+            ms = time_query(tree, q, k, QueryOpts.make(threads_per_query=g, prune_boxes=boxes, traversal=trav), reps)
+            table.append((L, g, boxes, trav, ms))
+            if best is None or ms < best[4]:
+                best = (L, g, boxes, trav, ms)
         del tree
-    ch = Choice(levels=best[0], threads_per_query=best[1], ms=best[3], plain_levels=L0, table=table,
-                prune_boxes=best[2])
+    ch = Choice(levels=best[0], threads_per_query=best[1], ms=best[4], plain_levels=L0, table=table,
+                prune_boxes=best[2], traversal=best[3])
     if use_cache:
         cache[key] = asdict(ch)
         _store_cache(cache)
@@ -119,6 +123,6 @@ def autotune(points_ref: torch.Tensor, queries: torch.Tensor, k: int,
 
 
 def build_tuned_kd_tree(points_ref: torch.Tensor, queries: torch.Tensor, k: int, **kw) -> TorchKDTree:
-    """build_kd_tree with the autotuned depth and lanes per query."""
+    """build_kd_tree with the autotuned depth and launch options."""
     ch = autotune(points_ref, queries, k, **kw)
     return build_kd_tree(points_ref, levels=ch.levels, query_opts=ch.opts())

@@ -23,7 +23,13 @@
 //  4. The k best keys live in registers, distributed over the group
 //     (TopK in tk_device.cuh); candidates are offered in lane order.
 //  5. Warps pull work from a global counter (persistent grid sized to the
-//     SM count), so no block waits for a slow neighbour.
+//     SM count), so no block waits for a slow neighbour.  A warp takes 32/G
+//     consecutive binned queries at once and finishes them together: handing
+//     a lane a new query as soon as its own ends was measured slower, as the
+//     lanes of a warp then stop sharing the leaves they load.
+//  6. Alternatively (k_kd_packet) the 32 queries of a warp walk the tree
+//     together, one lane each, which keeps the warp converged at the price of
+//     visiting the union of the lanes' leaves.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -246,8 +252,16 @@ __device__ __forceinline__ void kd_query_one(const KdArgs<T>& a, const T* s_med,
                           gbase);
 }
 
+constexpr int kKdBlock = 256;  // threads per block of the KD query kernels
+
+// Dynamic shared memory of the KD query kernels: the top split values.
+template <typename T>
+inline size_t kd_smem_bytes(int smem_levels) {
+    return sizeof(T) * ((size_t(1) << smem_levels) - 1);
+}
+
 template <typename T, int D, int G, int R>
-__global__ void __launch_bounds__(256) k_kd_query(const KdArgs<T> a) {
+__global__ void __launch_bounds__(kKdBlock) k_kd_query(const KdArgs<T> a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T* s_med = reinterpret_cast<T*>(smem_raw);
     const int n_smem = (1 << a.smem_levels) - 1;
@@ -271,6 +285,150 @@ __global__ void __launch_bounds__(256) k_kd_query(const KdArgs<T> a) {
             const int qi = a.order ? __ldg(a.order + t) : t;
             kd_query_one<T, D, G, R>(a, s_med, qi, gmask, gl, gbase);
         }
+        __syncwarp();
+    }
+}
+
+// ------------------------------------------------------- warp packets --
+//
+// Packet traversal: the 32 lanes of a warp each own one query (and their own
+// register list of R <= 16 keys), but walk the tree TOGETHER, so the warp
+// never diverges on the traversal itself.  Queries arrive binned by tree
+// cell, so the 32 queries of a warp are neighbours and need mostly the same
+// nodes.
+//  1. Each lane first descends to its own home leaf (L steps for every lane,
+//     no divergence) and fills its list from that leaf.
+//  2. The warp then runs one depth-first walk from the root.  A node is
+//     entered when its bounding box can still hold a neighbour of ANY lane
+//     (per-lane box_bound <= that lane's worst, ballot); the near child is
+//     the side most of the interested lanes fall on.  The stack of pending
+//     nodes is warp-uniform and lives one entry per lane in a register
+//     (depth-first with two pushes per internal node holds <= levels + 1
+//     entries, below 32).
+//  3. At a leaf every lane reads the same records (one broadcast load) and
+//     offers them to its own list; a lane skips its home leaf, whose points
+//     it has already offered.
+// A lane examines every point the per-query search would (a node it needs is
+// entered by the warp), plus others that cannot enter its list, so the
+// result is again the exhaustive (distance, original index) answer.
+
+template <typename T, int D, int R>
+__device__ __forceinline__ void kd_packet_search(const TreeView<T>& tv, const T (&q)[D], bool active, int k,
+                                                 T* out_d, int32_t* out_i, int lane) {
+    TopK<T, 1, R> list;
+    list.init(k, 0);
+    Key<T> worst = Key<T>::sentinel();
+    const int L = tv.levels;
+    const int first_leaf = (1 << L) - 1;
+
+    // 1. own descent and home leaf
+    int node = 0, ax = 0;
+    for (int depth = 0; depth < L; ++depth) {
+        const T m = depth < tv.smem_levels ? tv.s_med[node] : __ldg(tv.medians + node);
+        node = 2 * node + (pick<T, D>(q, ax) < m ? 1 : 2);  // src/kdtree.cpp:30
+        ax = (ax + 1 == D) ? 0 : ax + 1;
+    }
+    const int home = node - first_leaf;
+    {
+        int beg = __ldg(tv.leaf_off + home);
+        const int end = __ldg(tv.leaf_off + home + 1);
+        if (k == R && end - beg >= R) {
+            Key<T> v[R];
+#pragma unroll
+            for (int i = 0; i < R; ++i) {
+                const PointRec<T> p = load_rec(tv.pts + beg + i);
+                v[i] = Key<T>::make(sqdist<T, D>(q, p), rec_index(p));
+            }
+            bitonic_sort<T, R>(v);
+#pragma unroll
+            for (int i = 0; i < R; ++i) list.slot[i] = v[i];
+            worst = list.worst(0u);
+            beg += R;
+        }
+        for (int j = beg; j < end; ++j) {
+            const PointRec<T> p = load_rec(tv.pts + j);
+            worst = offer<T, 1, R>(list, Key<T>::make(sqdist<T, D>(q, p), rec_index(p)), worst, 0u, 0, 0);
+        }
+    }
+    // A lane without a query needs nothing more, and neither does a query
+    // with a NaN coordinate: all its distances are NaN, and a NaN key never
+    // enters the list (it orders above the sentinel).
+    bool nan_q = false;
+#pragma unroll
+    for (int c = 0; c < D; ++c) nan_q |= q[c] != q[c];
+    T worst_d = (active && !nan_q) ? worst.dist() : T(-1);
+
+    // 2./3. the warp's walk
+    int stk = 0;  // this lane's stack slot; slot `lane` of the warp's stack
+    int sp = 1;   // root on the stack
+    while (sp > 0) {
+        --sp;
+        const int nd = __shfl_sync(0xFFFFFFFFu, stk, sp);
+        const bool need = box_bound<T, D>(tv.boxes, nd, q) <= worst_d;
+        const unsigned needm = __ballot_sync(0xFFFFFFFFu, need);
+        if (!needm) continue;
+        if (nd < first_leaf) {
+            const int depth = 31 - __clz(nd + 1);
+            const int nax = depth % D;
+            const T m = depth < tv.smem_levels ? tv.s_med[nd] : __ldg(tv.medians + nd);
+            const unsigned leftm = __ballot_sync(0xFFFFFFFFu, need && pick<T, D>(q, nax) < m);
+            const bool near_left = 2 * __popc(leftm) >= __popc(needm);
+            const int nearc = 2 * nd + (near_left ? 1 : 2);
+            const int farc = 2 * nd + (near_left ? 2 : 1);
+            if (lane == sp) stk = farc;
+            if (lane == sp + 1) stk = nearc;
+            sp += 2;
+            continue;
+        }
+        const int leaf = nd - first_leaf;
+        const bool take = need && leaf != home;
+        if (!__any_sync(0xFFFFFFFFu, take)) continue;
+        const int beg = __ldg(tv.leaf_off + leaf);
+        const int end = __ldg(tv.leaf_off + leaf + 1);
+        int j = beg;
+        for (; j + 1 < end; j += 2) {
+            const PointRec<T> p0 = load_rec(tv.pts + j);
+            const PointRec<T> p1 = load_rec(tv.pts + j + 1);
+            const Key<T> k0 = Key<T>::make(sqdist<T, D>(q, p0), rec_index(p0));
+            const Key<T> k1 = Key<T>::make(sqdist<T, D>(q, p1), rec_index(p1));
+            if (take) {
+                worst = offer<T, 1, R>(list, k0, worst, 0u, 0, 0);
+                worst = offer<T, 1, R>(list, k1, worst, 0u, 0, 0);
+            }
+        }
+        if (j < end) {
+            const PointRec<T> p = load_rec(tv.pts + j);
+            const Key<T> k0 = Key<T>::make(sqdist<T, D>(q, p), rec_index(p));
+            if (take) worst = offer<T, 1, R>(list, k0, worst, 0u, 0, 0);
+        }
+        if (take) worst_d = worst.dist();
+    }
+    if (active) list.store(k, 0, out_d, out_i, 0);
+}
+
+template <typename T, int D, int R>
+__global__ void __launch_bounds__(256) k_kd_packet(const KdArgs<T> a) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* s_med = reinterpret_cast<T*>(smem_raw);
+    const int n_smem = (1 << a.smem_levels) - 1;
+    for (int i = threadIdx.x; i < n_smem; i += blockDim.x) s_med[i] = a.medians[i];
+    __syncthreads();
+
+    const int lane = threadIdx.x & 31;
+    const TreeView<T> tv{a.pts, a.medians, a.leaf_off, a.levels, a.smem_levels, s_med, a.boxes};
+    for (;;) {
+        int base = 0;
+        if (lane == 0) base = atomicAdd(a.work, 32);
+        base = __shfl_sync(0xFFFFFFFFu, base, 0);
+        if (base >= a.nq) break;
+        const int t = base + lane;
+        const bool active = t < a.nq;
+        const int qi = active ? (a.order ? __ldg(a.order + t) : t) : 0;
+        T q[D];
+#pragma unroll
+        for (int c = 0; c < D; ++c) q[c] = active ? a.q[(long long)qi * D + c] : T(0);
+        kd_packet_search<T, D, R>(tv, q, active, a.k, a.out_d + (long long)qi * a.k,
+                                  a.out_i + (long long)qi * a.k, lane);
         __syncwarp();
     }
 }
@@ -310,6 +468,10 @@ template <typename T, int D>
 int kd_query_launch(const KdArgs<T>& a, const KdLaunch& l, cudaStream_t s);
 template <typename T, int D>
 const void* kd_query_kernel(int G, int R);
+template <typename T, int D>
+int kd_packet_launch(const KdArgs<T>& a, const KdLaunch& l, cudaStream_t s);  // uses l.R only
+template <typename T, int D>
+const void* kd_packet_kernel(int R);
 template <typename T, int D>
 void bin_count_launch(const T* q, int nq, const T* medians, int B, int* counts, int* bin_of, int* pos_of,
                       cudaStream_t s);

@@ -122,24 +122,30 @@ int pow2_ceil(int v) {
 template <typename T, int D>
 int run_query(const tk_tree* t, const T* q, int nq, int k, T* dists, int32_t* idx, const tk_query_opts& o,
               char* ws, cudaStream_t s) {
+    if (o.traversal < 0 || o.traversal > 2) return fail(TK_EINVAL, "traversal must be 0, 1 or 2");
+    // warp packets: one lane per query, the warp walks the tree together
+    const bool packet = o.traversal == 2 && k <= 16 && t->d_boxes != nullptr;
     // lanes per query and registers per lane
-    int G = o.threads_per_query > 0 ? o.threads_per_query : auto_lanes(t);
-    if (G != 1 && G != 2 && G != 4 && G != 8 && G != 16 && G != 32)
-        return fail(TK_EINVAL, "threads_per_query must be 1, 2, 4, 8, 16 or 32");
-    G = std::max(G, pow2_ceil((k + 15) / 16));
-    int R = pow2_ceil((k + G - 1) / G);
-    while (!gr_available(t->dtype, D, G, R) && G < 32) {
-        G <<= 1;
+    int G = 1, R = pow2_ceil(k);
+    if (!packet) {
+        G = o.threads_per_query > 0 ? o.threads_per_query : auto_lanes(t);
+        if (G != 1 && G != 2 && G != 4 && G != 8 && G != 16 && G != 32)
+            return fail(TK_EINVAL, "threads_per_query must be 1, 2, 4, 8, 16 or 32");
+        G = std::max(G, pow2_ceil((k + 15) / 16));
         R = pow2_ceil((k + G - 1) / G);
+        while (!gr_available(t->dtype, D, G, R) && G < 32) {
+            G <<= 1;
+            R = pow2_ceil((k + G - 1) / G);
+        }
+        if (!gr_available(t->dtype, D, G, R)) return fail(TK_EUNSUPPORTED, "no kernel shape for this k");
     }
-    if (!gr_available(t->dtype, D, G, R)) return fail(TK_EUNSUPPORTED, "no kernel shape for this k");
 
     const int L = t->levels;
     int S = o.smem_levels >= 0 ? o.smem_levels : (sizeof(T) == 4 ? 12 : 11);
     S = std::max(0, std::min({S, L, sizeof(T) == 4 ? 15 : 14}));  // <= 128 KiB of shared memory
-    const int block = 256;
-    const size_t smem = sizeof(T) * ((size_t(1) << S) - 1);
-    const void* kfn = kd_query_kernel<T, D>(G, R);
+    const int block = kKdBlock;
+    const size_t smem = kd_smem_bytes<T>(S);
+    const void* kfn = packet ? kd_packet_kernel<T, D>(R) : kd_query_kernel<T, D>(G, R);
     if (!kfn) return fail(TK_EUNSUPPORTED, "KD query kernel shape not compiled");
     if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
@@ -183,7 +189,7 @@ int run_query(const tk_tree* t, const T* q, int nq, int k, T* dists, int32_t* id
     a.pts = static_cast<const PointRec<T>*>(t->d_pts);
     a.medians = static_cast<const T*>(t->d_medians);
     a.leaf_off = t->d_leaf_off;
-    a.boxes = o.prune_boxes == 0 ? nullptr : static_cast<const PointRec<T>*>(t->d_boxes);
+    a.boxes = (o.prune_boxes == 0 && !packet) ? nullptr : static_cast<const PointRec<T>*>(t->d_boxes);
     a.levels = L;
     a.smem_levels = S;
     a.q = q;
@@ -195,7 +201,7 @@ int run_query(const tk_tree* t, const T* q, int nq, int k, T* dists, int32_t* id
     a.work = counter;
     KdLaunch l{G, R, block, grid, smem};
     if (o.kernel_start_event) cudaEventRecord(static_cast<cudaEvent_t>(o.kernel_start_event), s);
-    const int rc = kd_query_launch<T, D>(a, l, s);
+    const int rc = packet ? kd_packet_launch<T, D>(a, l, s) : kd_query_launch<T, D>(a, l, s);
     if (rc == TK_OK && o.kernel_stop_event) cudaEventRecord(static_cast<cudaEvent_t>(o.kernel_stop_event), s);
     return rc;
 }
@@ -389,7 +395,7 @@ int tk_tree_query(const tk_tree* t, const void* q, int64_t nq, int k, void* dist
     const size_t need = ws_layout(t->levels, nq).total;
     if (!workspace || workspace_bytes < need)
         return fail(TK_EWORKSPACE, "workspace too small: need " + std::to_string(need) + " bytes");
-    tk_query_opts o{0, -1, -1, 0, 0, nullptr, nullptr, -1};
+    tk_query_opts o{0, -1, -1, 0, 0, nullptr, nullptr, -1, 0};
     if (opts) o = *opts;
     DeviceGuard g(t->device);
     cudaStream_t s = static_cast<cudaStream_t>(stream);
@@ -474,7 +480,7 @@ extern "C" int tk_tree_query_noalloc(const tk_tree* t, const void* q, int64_t nq
     if (rc != TK_OK) return rc;
     if (ws_layout(t->levels, nq).total > kNoAllocScratchBytes)
         return fail(TK_EINVAL, "query needs more scratch than the static array holds");
-    tk_query_opts o{0, -1, -1, 0, 0, nullptr, nullptr, -1};
+    tk_query_opts o{0, -1, -1, 0, 0, nullptr, nullptr, -1, 0};
     if (opts) o = *opts;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     char* ws = static_cast<char*>(scratch);
