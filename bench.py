@@ -220,10 +220,16 @@ def run_ours(args, rank, world):
     ref = torch.from_numpy(ref_np).to(dev)
     q = torch.from_numpy(q_np).to(dev)
 
-    # ---- plain: reference heuristic depth, default launch shape
+    # ---- plain: reference heuristic depth, default launch shape, built on the host like the reference
     t0 = time.perf_counter()
-    plain = tk.build_kd_tree(ref)
+    plain = tk.build_kd_tree(ref, build="host")
     build_plain_s = time.perf_counter() - t0
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    del_me = tk.build_kd_tree(ref, build="device", levels=plain.levels)
+    torch.cuda.synchronize()
+    build_plain_dev_s = time.perf_counter() - t0
+    del del_me
     # ---- chosen: autotuned depth and lanes per query (or given on the command line)
     t0 = time.perf_counter()
     if args.levels and args.tpq:
@@ -233,8 +239,10 @@ def run_ours(args, rank, world):
     else:
         ch = autotune(ref, q, K_NN, use_cache=False)
     tune_s = time.perf_counter() - t0
+    torch.cuda.synchronize()
     t0 = time.perf_counter()
-    chosen = tk.build_kd_tree(ref, levels=ch.levels, query_opts=ch.opts())
+    chosen = tk.build_kd_tree(ref, levels=ch.levels, query_opts=ch.opts(), build="device")
+    torch.cuda.synchronize()
     build_chosen_s = time.perf_counter() - t0
 
     if args.profile:
@@ -364,7 +372,9 @@ def run_ours(args, rank, world):
                    "prune_boxes": ch.prune_boxes, "traversal": {1: "per-query stacks", 2: "warp packets"}[ch.traversal],
                    "graph_captured": True, "l2": f"flushed between steps ({L2_FLUSH_BYTES >> 20} MiB write)",
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
-                   "tree_build_s": {"plain": build_plain_s, "chosen": build_chosen_s}, "autotune_s": tune_s},
+                   "tree_build_s": {f"host_L{plain.levels}": build_plain_s,
+                                    f"device_L{plain.levels}": build_plain_dev_s,
+                                    f"device_L{ch.levels}": build_chosen_s}, "autotune_s": tune_s},
         "plain": {"value": plain_value, "ms_per_step": t_plain / args.steps, "levels": plain.levels,
                   "threads_per_query": "auto"},
         "chosen_vs_plain": value / plain_value,

@@ -71,6 +71,21 @@ typedef struct tk_tree_info {
 int tk_tree_create(const void* host_points, int64_t n, int dims, int dtype, int levels, int device,
                    int n_threads, tk_tree** out);
 
+/* Build the same tree ON THE GPU from device-resident points: dev_points is
+ * device memory on `device`, [n, dims] C-contiguous, float or double per
+ * dtype.  The result is identical to tk_tree_create's (split values, leaf
+ * offsets, point order, original indices; ties on a coordinate ordered by
+ * original index), built level by level from one stable radix sort per axis
+ * instead of per-node sorts, with no host copy of the points.  Runs on
+ * `stream` and synchronises it before returning.  The layout getters below
+ * copy from the device for such a tree.  Same errors as tk_tree_create
+ * (NaN points, too many levels for n).  Replaces the host-side
+ * createKDTree (src/kdtree.hpp:494-534) + copyPartitionToGPU
+ * (src/kdtree_g.cu:63-98) that the reference runs after copying the points
+ * to the host (torch_kdtree/nn_distance.py:26-31). */
+int tk_tree_create_device(const void* dev_points, int64_t n, int dims, int dtype, int levels, int device,
+                          void* stream, tk_tree** out);
+
 /* Free the tree and its device memory.  Replaces ~KDTree
  * (src/interface.cpp:88-94) + freePartitionFromGPU (src/kdtree_g.cu:140-157). */
 int tk_tree_destroy(tk_tree* tree);

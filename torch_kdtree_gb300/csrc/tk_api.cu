@@ -257,6 +257,35 @@ void free_tree_device(tk_tree* t) {
     t->d_leaf_off = nullptr;
 }
 
+// Layout of a tree built on the GPU: points (T[n*dims]) and / or the
+// permutation (int32[n]) copied out of its device point records.
+template <typename T>
+int device_layout(const tk_tree* t, T* points, int32_t* perm) {
+    DeviceGuard g(t->device);
+    std::vector<PointRec<T>> recs(static_cast<size_t>(t->n));
+    const cudaError_t e = cudaMemcpy(recs.data(), t->d_pts, sizeof(PointRec<T>) * recs.size(), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return fail(TK_ECUDA, std::string("layout copy: ") + cudaGetErrorString(e));
+    for (int64_t i = 0; i < t->n; ++i) {
+        const PointRec<T>& r = recs[size_t(i)];
+        if (points) {
+            const T c[3] = {r.x, r.y, r.z};
+            for (int d = 0; d < t->dims; ++d) points[i * t->dims + d] = c[d];
+        }
+        if (perm) {
+            if (sizeof(T) == 4) {
+                uint32_t bits;
+                std::memcpy(&bits, &r.w, 4);
+                perm[i] = int32_t(bits);
+            } else {
+                uint64_t bits;
+                std::memcpy(&bits, &r.w, 8);
+                perm[i] = int32_t(bits);
+            }
+        }
+    }
+    return TK_OK;
+}
+
 }  // namespace
 }  // namespace tk
 
@@ -322,6 +351,58 @@ int tk_tree_create(const void* host_points, int64_t n, int dims, int dtype, int 
     return TK_OK;
 }
 
+int tk_tree_create_device(const void* dev_points, int64_t n, int dims, int dtype, int levels, int device,
+                          void* stream, tk_tree** out) {
+    clear_error();
+    if (!out) return fail(TK_EINVAL, "out is null");
+    *out = nullptr;
+    if (dtype != TK_F32 && dtype != TK_F64) return fail(TK_EINVAL, "dtype must be TK_F32 or TK_F64");
+    if (!dev_points) return fail(TK_EINVAL, "points pointer is null");
+    if (dims < 1 || dims > 3)
+        return fail(TK_EINVAL, "KD-tree supports dims 1, 2 or 3 (got " + std::to_string(dims) + ")");
+    if (n < 1) return fail(TK_EINVAL, "the reference point cloud is empty");
+    if (n >= (int64_t(1) << 31)) return fail(TK_EINVAL, "only 32 bit signed indexing implemented (n < 2^31)");
+    if (levels < 1 || levels > kMaxLevels)
+        return fail(TK_EINVAL, "levels must be in [1, " + std::to_string(kMaxLevels) + "]");
+    // node sizes at depth t are floor / ceil of n / 2^t: a leaf parent gets no
+    // point exactly when n < 2^(levels-1)
+    if (n < (int64_t(1) << (levels - 1)))
+        return fail(TK_EINVAL,
+                    "Ran out of points while building KD-Tree. Either you required too many levels, "
+                    "or you used a lot of coplanar points");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) {
+        cudaGetLastError();
+        return fail(TK_EINVAL, "CUDA device " + std::to_string(device) + " is not available");
+    }
+    cudaPointerAttributes attr;
+    if (cudaPointerGetAttributes(&attr, dev_points) != cudaSuccess ||
+        (attr.type != cudaMemoryTypeDevice && attr.type != cudaMemoryTypeManaged) || attr.device != device) {
+        cudaGetLastError();
+        return fail(TK_EINVAL, "points must be device memory on CUDA device " + std::to_string(device));
+    }
+    tk_tree* t = new (std::nothrow) tk_tree();
+    if (!t) return fail(TK_ENOMEM, "host allocation failed");
+    t->dtype = dtype;
+    t->dims = dims;
+    t->levels = levels;
+    t->device = device;
+    t->n = n;
+    t->host_layout = false;
+    DeviceGuard g(device);
+    const int rc = dtype == TK_F32
+                       ? build_device_tree<float>(static_cast<const float*>(dev_points), n, dims, levels, stream, t)
+                       : build_device_tree<double>(static_cast<const double*>(dev_points), n, dims, levels, stream, t);
+    if (rc != TK_OK) {
+        cudaStreamSynchronize(static_cast<cudaStream_t>(stream));
+        free_tree_device(t);
+        delete t;
+        return rc;
+    }
+    *out = t;
+    return TK_OK;
+}
+
 int tk_tree_destroy(tk_tree* t) {
     clear_error();
     if (!t) return TK_OK;
@@ -347,6 +428,8 @@ int tk_tree_get_info(const tk_tree* t, tk_tree_info* out) {
 
 int tk_tree_get_perm(const tk_tree* t, int32_t* out) {
     if (!t || !out) return fail(TK_EINVAL, "null argument");
+    if (!t->host_layout)
+        return t->dtype == TK_F32 ? device_layout<float>(t, nullptr, out) : device_layout<double>(t, nullptr, out);
     const auto& p = t->dtype == TK_F32 ? t->h32.perm : t->h64.perm;
     std::memcpy(out, p.data(), sizeof(int32_t) * p.size());
     return TK_OK;
@@ -354,6 +437,9 @@ int tk_tree_get_perm(const tk_tree* t, int32_t* out) {
 
 int tk_tree_get_points(const tk_tree* t, void* out) {
     if (!t || !out) return fail(TK_EINVAL, "null argument");
+    if (!t->host_layout)
+        return t->dtype == TK_F32 ? device_layout<float>(t, static_cast<float*>(out), nullptr)
+                                  : device_layout<double>(t, static_cast<double*>(out), nullptr);
     if (t->dtype == TK_F32)
         std::memcpy(out, t->h32.structured.data(), sizeof(float) * t->h32.structured.size());
     else
@@ -363,6 +449,17 @@ int tk_tree_get_points(const tk_tree* t, void* out) {
 
 int tk_tree_get_splits(const tk_tree* t, void* medians, int32_t* leaf_offsets) {
     if (!t) return fail(TK_EINVAL, "null argument");
+    if (!t->host_layout) {
+        DeviceGuard g(t->device);
+        const size_t nparts = (size_t(1) << t->levels) - 1;
+        cudaError_t e = cudaSuccess;
+        if (medians)
+            e = cudaMemcpy(medians, t->d_medians, (t->dtype == TK_F32 ? 4 : 8) * nparts, cudaMemcpyDeviceToHost);
+        if (e == cudaSuccess && leaf_offsets)
+            e = cudaMemcpy(leaf_offsets, t->d_leaf_off, sizeof(int32_t) * (nparts + 2), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return fail(TK_ECUDA, std::string("split copy: ") + cudaGetErrorString(e));
+        return TK_OK;
+    }
     if (medians) {
         if (t->dtype == TK_F32)
             std::memcpy(medians, t->h32.medians.data(), sizeof(float) * t->h32.medians.size());

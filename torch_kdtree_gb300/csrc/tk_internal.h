@@ -41,6 +41,17 @@ int build_host_tree(const T* pts, int64_t n, int dims, int levels, int n_threads
 
 }  // namespace tk
 
+struct tk_tree;
+
+namespace tk {
+// Builds the tree on the GPU from device points straight into t's device
+// image (tree_build_gpu.cu), same layout as build_host_tree.  The arguments
+// are validated by the caller; runs on and synchronises the CUDA stream
+// `stream` before returning.
+template <typename T>
+int build_device_tree(const T* pts, int64_t n, int dims, int levels, void* stream, tk_tree* t);
+}  // namespace tk
+
 // Opaque handle behind the C ABI.
 struct tk_tree {
     int dtype = TK_F32;
@@ -48,7 +59,10 @@ struct tk_tree {
     int levels = 0;
     int device = 0;
     int64_t n = 0;
-    // host layout (one of the two is filled)
+    // host layout (one of the two is filled when the tree was built on the
+    // host; a tree built on the GPU keeps only its device image and the
+    // layout getters copy from there)
+    bool host_layout = true;
     tk::HostTree<float> h32;
     tk::HostTree<double> h64;
     // device image

@@ -1,6 +1,6 @@
 """Python API of the engine, mirroring torch_kdtree's (torch_kdtree/nn_distance.py).
 
-    tree = build_kd_tree(points_ref)                 # KD-tree built on the host, uploaded once
+    tree = build_kd_tree(points_ref)                 # KD-tree in the reference's layout, on the GPU
     dists, inds = tree.query(points_query, nr_nns_searches=k)
 
 Same names, argument meaning and error behaviour as the reference:
@@ -52,14 +52,28 @@ def _workspace(nbytes: int, device: torch.device) -> torch.Tensor:
 
 
 class _Tree:
-    """Owner of a tk_tree handle."""
+    """Owner of a tk_tree handle: built on the host from a numpy array, or
+    (``from_device``) on the GPU from a CUDA tensor."""
 
-    def __init__(self, points: np.ndarray, levels: int, device_index: int):
+    def __init__(self, points: Optional[np.ndarray], levels: int, device_index: int):
+        self.handle = None
+        if points is None:
+            return
         n, d = points.shape
         dt = _lib.TK_F32 if points.dtype == np.float32 else _lib.TK_F64
         h = ctypes.c_void_p()
         check(LIB.tk_tree_create(points.ctypes.data, n, d, dt, levels, device_index, 0, ctypes.byref(h)))
         self.handle = h
+
+    @classmethod
+    def from_device(cls, points: torch.Tensor, levels: int) -> "_Tree":
+        t = cls(None, levels, points.device.index)
+        n, d = points.shape
+        h = ctypes.c_void_p()
+        check(LIB.tk_tree_create_device(points.data_ptr(), n, d, _DTYPES[points.dtype], levels, points.device.index,
+                                        _stream_ptr(points.device), ctypes.byref(h)))
+        t.handle = h
+        return t
 
     def info(self) -> TreeInfo:
         info = TreeInfo()
@@ -86,7 +100,7 @@ def knn_query_raw(tree: _Tree, q: torch.Tensor, k: int, dists: torch.Tensor, idx
 
 class TorchKDTree:
     def __init__(self, points_ref: torch.Tensor, device: torch.device, levels: int, squared_distances: bool,
-                 query_opts: Optional[QueryOpts] = None):
+                 query_opts: Optional[QueryOpts] = None, build: str = "auto"):
         """Builds the KD-tree.  See :func:`build_kd_tree`."""
         if device.type != "cuda":
             raise RuntimeError(
@@ -105,8 +119,17 @@ class TorchKDTree:
             device = torch.device("cuda", torch.cuda.current_device())
         self.device = device
         self.levels = int(levels)
-        host = np.ascontiguousarray(points_ref.detach().cpu().numpy())
-        self._tree = _Tree(host, self.levels, device.index)
+        if build not in ("auto", "host", "device"):
+            raise ValueError("build must be 'auto', 'host' or 'device'")
+        if build == "auto":
+            build = "device" if points_ref.is_cuda else "host"
+        self.built_on = build
+        if build == "device":
+            pts = points_ref.detach().to(device).contiguous()
+            self._tree = _Tree.from_device(pts, self.levels)
+        else:
+            host = np.ascontiguousarray(points_ref.detach().cpu().numpy())
+            self._tree = _Tree(host, self.levels, device.index)
         self.dtype_idx = torch.int32
         self.ref_requires_grad = points_ref.requires_grad
         self.points_ref_bak = points_ref
@@ -188,10 +211,13 @@ class TorchKDTree:
 
 def build_kd_tree(points_ref: Union[torch.Tensor, np.ndarray], device: Optional[torch.device] = None,
                   squared_distances: bool = True, levels: Optional[int] = None,
-                  query_opts: Optional[QueryOpts] = None) -> TorchKDTree:
+                  query_opts: Optional[QueryOpts] = None, build: str = "auto") -> TorchKDTree:
     """Builds the KD-tree for subsequent queries (torch_kdtree/nn_distance.py:119-160).
 
-    The tree is built on the host in the reference's layout and uploaded once.
+    The tree has the reference's layout and lives on the GPU.  ``build``:
+    "host" builds it on the CPU (as the reference does) and uploads it once;
+    "device" builds it on the GPU from the CUDA tensor (same layout, no host
+    copy); "auto" (default) picks "device" for CUDA input, else "host".
     ``device`` defaults to ``points_ref.device`` (which must then be CUDA);
     ``levels`` defaults to the reference's heuristic and may range 1..24."""
     if issubclass(type(points_ref), np.ndarray):
@@ -206,7 +232,7 @@ def build_kd_tree(points_ref: Union[torch.Tensor, np.ndarray], device: Optional[
     assert issubclass(type(points_ref), torch.Tensor)
     assert device.type != "cuda" or gpu_available, "You requested the KD-Tree on the GPU, but no CUDA device is visible"
     assert device.type in ["cuda", "cpu"]
-    return TorchKDTree(points_ref, device, levels, squared_distances, query_opts)
+    return TorchKDTree(points_ref, device, levels, squared_distances, query_opts, build)
 
 
 _BRUTE_MODES = {"exact": _lib.TK_BRUTE_EXACT, "fp32": _lib.TK_BRUTE_EXACT, "fp64": _lib.TK_BRUTE_EXACT,
