@@ -71,6 +71,19 @@ typedef struct tk_tree_info {
 int tk_tree_create(const void* host_points, int64_t n, int dims, int dtype, int levels, int device,
                    int n_threads, tk_tree** out);
 
+/* Re-create a tree from a saved layout (the arrays the getters below
+ * return: structured points T[n*dims], perm int32[n], split values
+ * T[2^L-1], leaf offsets int32[2^L+1]; all host memory) without rebuilding
+ * it.  The layout is validated -- offsets from 0 to n and non-decreasing,
+ * perm a permutation, no NaN, every split value separating its children's
+ * points along its axis -- and TK_EINVAL is returned otherwise, so a
+ * corrupt file cannot make queries silently inexact.  device: CUDA ordinal
+ * or -1 (host-only).  No reference counterpart: the reference always
+ * rebuilt the tree (src/interface.cpp:25-43). */
+int tk_tree_create_from_layout(const void* structured_points, const int32_t* perm, const void* medians,
+                               const int32_t* leaf_offsets, int64_t n, int dims, int dtype, int levels, int device,
+                               tk_tree** out);
+
 /* Build the same tree ON THE GPU from device-resident points: dev_points is
  * device memory on `device`, [n, dims] C-contiguous, float or double per
  * dtype.  The result is identical to tk_tree_create's (split values, leaf

@@ -133,3 +133,65 @@ def test_default_levels_matches_reference_heuristic():
     from torch_kdtree_gb300 import default_levels
     for n, L in [(5, 1), (30, 1), (1000, 6), (100_000, 13), (4_194_304, 13), (16, 1), (128, 4)]:
         assert default_levels(n) == L
+
+
+def tree_from_layout(pts, perm, med, off, levels, device=-1):
+    from torch_kdtree_gb300._lib import LIB
+    h = ctypes.c_void_p()
+    dt = 0 if pts.dtype == np.float32 else 1
+    st = LIB.tk_tree_create_from_layout(pts.ctypes.data, perm.ctypes.data, med.ctypes.data, off.ctypes.data,
+                                        pts.shape[0], pts.shape[1], dt, levels, device, ctypes.byref(h))
+    return st, h
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+@pytest.mark.parametrize("d", [1, 2, 3])
+def test_layout_round_trip_and_validation(dtype, d):
+    """A saved layout re-creates the same tree; corrupt layouts are refused
+    (a tree whose splits do not separate its points would give inexact
+    answers, so it must not load)."""
+    from torch_kdtree_gb300._lib import LIB, TK_EINVAL, check
+    rng = np.random.default_rng(30 + d)
+    ref = rng.standard_normal((3000, d)).astype(dtype)
+    L = 7
+    st, h = host_tree(ref, L)
+    check(st)
+    try:
+        pts, perm, med, off = layout_of(h, 3000, d, L, ref.dtype)
+    finally:
+        LIB.tk_tree_destroy(h)
+    st, h2 = tree_from_layout(pts, perm, med, off, L)
+    check(st)
+    try:
+        again = layout_of(h2, 3000, d, L, ref.dtype)
+    finally:
+        LIB.tk_tree_destroy(h2)
+    for a, b in zip((pts, perm, med, off), again):
+        np.testing.assert_array_equal(a, b)
+
+    def refused(p=pts, pe=perm, m=med, o=off, lv=L):
+        st, hh = tree_from_layout(np.ascontiguousarray(p), np.ascontiguousarray(pe), np.ascontiguousarray(m),
+                                  np.ascontiguousarray(o), lv)
+        if hh.value:
+            LIB.tk_tree_destroy(hh)
+        return st == TK_EINVAL
+
+    bad_perm = perm.copy()
+    bad_perm[5] = bad_perm[6]
+    assert refused(pe=bad_perm)
+    bad_off = off.copy()
+    bad_off[3] = bad_off[4] + 1  # decreasing offsets
+    assert refused(o=bad_off)
+    bad_end = off.copy()
+    bad_end[-1] -= 1
+    assert refused(o=bad_end)
+    nan_pts = pts.copy()
+    nan_pts[10, 0] = np.nan
+    assert refused(p=nan_pts)
+    moved = pts.copy()
+    moved[0, 0] = med[0] + abs(med[0]) + 10  # first point belongs left of the root split along axis 0
+    assert refused(p=moved)
+    wrong_split = med.copy()
+    wrong_split[0] = pts[:, 0].max() + 1
+    assert refused(m=wrong_split)
+    assert not refused(lv=L)

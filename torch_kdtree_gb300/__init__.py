@@ -4,7 +4,9 @@
     tree = build_kd_tree(points_ref)            # on a CUDA device
     dists, inds = tree.query(points_query, nr_nns_searches=k)
 """
-from .nn_distance import TorchKDTree, build_kd_tree, default_levels, gpu_available, nn_distance
+from .nn_distance import (TorchKDTree, build_kd_tree, default_levels, gpu_available, load_kd_tree, nn_distance,
+                          nn_distance_bidirectional)
 
-__all__ = ["build_kd_tree", "gpu_available", "TorchKDTree", "default_levels", "nn_distance"]
+__all__ = ["build_kd_tree", "gpu_available", "TorchKDTree", "default_levels", "load_kd_tree", "nn_distance",
+           "nn_distance_bidirectional"]
 __version__ = "0.1.0"

@@ -72,6 +72,7 @@ SIGNATURES = {
     "tk_cuda_available": (_int, []),
     "tk_tree_create": (_int, [_vp, _i64, _int, _int, _int, _int, _int, ctypes.POINTER(_vp)]),
     "tk_tree_create_device": (_int, [_vp, _i64, _int, _int, _int, _int, _vp, ctypes.POINTER(_vp)]),
+    "tk_tree_create_from_layout": (_int, [_vp, _vp, _vp, _vp, _i64, _int, _int, _int, _int, ctypes.POINTER(_vp)]),
     "tk_tree_destroy": (_int, [_vp]),
     "tk_tree_get_info": (_int, [_vp, ctypes.POINTER(TreeInfo)]),
     "tk_tree_get_perm": (_int, [_vp, _vp]),

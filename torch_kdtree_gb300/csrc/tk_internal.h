@@ -39,6 +39,13 @@ struct HostTree {
 template <typename T>
 int build_host_tree(const T* pts, int64_t n, int dims, int levels, int n_threads, HostTree<T>& out);
 
+// Takes over a saved layout (tree_build.cpp): validates it (leaf offsets,
+// permutation, no NaN, every split separating its children) and computes
+// the node boxes.  Returns TK_OK or sets the error.
+template <typename T>
+int tree_from_layout(const T* structured, const int32_t* perm, const T* medians, const int32_t* leaf_off, int64_t n,
+                     int dims, int levels, HostTree<T>& out);
+
 }  // namespace tk
 
 struct tk_tree;

@@ -88,6 +88,35 @@ struct Builder {
     }
 };
 
+// Tight bounding box of every node's points: leaves from their points,
+// inner nodes from their children; heap order over all 2^(L+1) - 1 nodes.
+template <typename T>
+void compute_boxes(HostTree<T>& out) {
+    const int64_t nleaves = int64_t(1) << out.levels;
+    const int64_t nnodes = 2 * nleaves - 1;
+    const T inf = std::numeric_limits<T>::infinity();
+    out.box_lo.assign(static_cast<size_t>(nnodes) * 3, inf);
+    out.box_hi.assign(static_cast<size_t>(nnodes) * 3, -inf);
+    for (int64_t l = 0; l < nleaves; ++l) {
+        const int64_t node = nleaves - 1 + l;
+        T* lo = &out.box_lo[node * 3];
+        T* hi = &out.box_hi[node * 3];
+        for (int32_t i = out.leaf_off[l]; i < out.leaf_off[l + 1]; ++i)
+            for (int c = 0; c < out.dims; ++c) {
+                const T v = out.structured[size_t(i) * out.dims + c];
+                lo[c] = std::min(lo[c], v);
+                hi[c] = std::max(hi[c], v);
+            }
+        if (out.leaf_off[l + 1] > out.leaf_off[l])
+            for (int c = out.dims; c < 3; ++c) lo[c] = hi[c] = T(0);  // unused coordinates are 0
+    }
+    for (int64_t node = nleaves - 2; node >= 0; --node)
+        for (int c = 0; c < 3; ++c) {
+            out.box_lo[node * 3 + c] = std::min(out.box_lo[(2 * node + 1) * 3 + c], out.box_lo[(2 * node + 2) * 3 + c]);
+            out.box_hi[node * 3 + c] = std::max(out.box_hi[(2 * node + 1) * 3 + c], out.box_hi[(2 * node + 2) * 3 + c]);
+        }
+}
+
 }  // namespace
 
 template <typename T>
@@ -138,29 +167,64 @@ int build_host_tree(const T* pts, int64_t n, int dims, int levels, int n_threads
         for (int c = 0; c < dims; ++c) out.structured[i * dims + c] = recs[i].c[c];
         out.perm[i] = recs[i].orig;
     }
-    // bounding boxes: leaves from their points, inner nodes from their children
-    const int64_t nleaves = int64_t(1) << levels;
-    const int64_t nnodes = 2 * nleaves - 1;
-    const T inf = std::numeric_limits<T>::infinity();
-    out.box_lo.assign(static_cast<size_t>(nnodes) * 3, inf);
-    out.box_hi.assign(static_cast<size_t>(nnodes) * 3, -inf);
-    for (int64_t l = 0; l < nleaves; ++l) {
-        const int64_t node = nleaves - 1 + l;
-        T* lo = &out.box_lo[node * 3];
-        T* hi = &out.box_hi[node * 3];
-        for (int32_t i = out.leaf_off[l]; i < out.leaf_off[l + 1]; ++i)
-            for (int c = 0; c < 3; ++c) {
-                lo[c] = std::min(lo[c], recs[i].c[c]);
-                hi[c] = std::max(hi[c], recs[i].c[c]);
-            }
-    }
-    for (int64_t node = nleaves - 2; node >= 0; --node)
-        for (int c = 0; c < 3; ++c) {
-            out.box_lo[node * 3 + c] = std::min(out.box_lo[(2 * node + 1) * 3 + c], out.box_lo[(2 * node + 2) * 3 + c]);
-            out.box_hi[node * 3 + c] = std::max(out.box_hi[(2 * node + 1) * 3 + c], out.box_hi[(2 * node + 2) * 3 + c]);
-        }
+    compute_boxes(out);
     return TK_OK;
 }
+
+template <typename T>
+int tree_from_layout(const T* structured, const int32_t* perm, const T* medians, const int32_t* leaf_off, int64_t n,
+                     int dims, int levels, HostTree<T>& out) {
+    if (!structured || !perm || !medians || !leaf_off) return fail(TK_EINVAL, "layout pointer is null");
+    if (dims < 1 || dims > 3)
+        return fail(TK_EINVAL, "KD-tree supports dims 1, 2 or 3 (got " + std::to_string(dims) + ")");
+    if (n < 1) return fail(TK_EINVAL, "the reference point cloud is empty");
+    if (n >= (int64_t(1) << 31)) return fail(TK_EINVAL, "only 32 bit signed indexing implemented (n < 2^31)");
+    if (levels < 1 || levels > kMaxLevels)
+        return fail(TK_EINVAL, "levels must be in [1, " + std::to_string(kMaxLevels) + "]");
+    const int64_t nleaves = int64_t(1) << levels;
+    const int64_t nparts = nleaves - 1;
+    // leaf offsets: from 0 to n, non-decreasing
+    if (leaf_off[0] != 0 || leaf_off[nleaves] != n) return fail(TK_EINVAL, "leaf offsets must run from 0 to n");
+    for (int64_t l = 0; l < nleaves; ++l)
+        if (leaf_off[l + 1] < leaf_off[l]) return fail(TK_EINVAL, "leaf offsets must be non-decreasing");
+    // perm: a permutation of 0..n-1
+    std::vector<unsigned char> seen(static_cast<size_t>(n), 0);
+    for (int64_t i = 0; i < n; ++i) {
+        const int32_t p = perm[i];
+        if (p < 0 || p >= n || seen[size_t(p)]) return fail(TK_EINVAL, "perm is not a permutation of 0..n-1");
+        seen[size_t(p)] = 1;
+    }
+    for (int64_t i = 0; i < n * dims; ++i)
+        if (std::isnan(structured[i])) return fail(TK_EINVAL, "reference points contain NaN");
+    for (int64_t i = 0; i < nparts; ++i)
+        if (std::isnan(medians[i])) return fail(TK_EINVAL, "split values contain NaN");
+    out.n = n;
+    out.dims = dims;
+    out.levels = levels;
+    out.structured.assign(structured, structured + n * dims);
+    out.perm.assign(perm, perm + n);
+    out.medians.assign(medians, medians + nparts);
+    out.leaf_off.assign(leaf_off, leaf_off + nleaves + 1);
+    compute_boxes(out);
+    // Every split must separate its children along its axis (left <= split <=
+    // right, the property the search's plane bounds rely on); otherwise the
+    // answers would silently stop being exact.
+    for (int64_t node = 0; node < nparts; ++node) {
+        const int depth = 63 - __builtin_clzll(uint64_t(node + 1));
+        const int ax = depth % dims;
+        const T m = out.medians[size_t(node)];
+        const T left_hi = out.box_hi[size_t(2 * node + 1) * 3 + ax];
+        const T right_lo = out.box_lo[size_t(2 * node + 2) * 3 + ax];
+        if (left_hi > m || right_lo < m)
+            return fail(TK_EINVAL, "layout is inconsistent: points on the wrong side of split " + std::to_string(node));
+    }
+    return TK_OK;
+}
+
+template int tree_from_layout<float>(const float*, const int32_t*, const float*, const int32_t*, int64_t, int, int,
+                                     HostTree<float>&);
+template int tree_from_layout<double>(const double*, const int32_t*, const double*, const int32_t*, int64_t, int, int,
+                                      HostTree<double>&);
 
 template int build_host_tree<float>(const float*, int64_t, int, int, int, HostTree<float>&);
 template int build_host_tree<double>(const double*, int64_t, int, int, int, HostTree<double>&);

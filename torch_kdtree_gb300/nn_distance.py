@@ -108,28 +108,34 @@ class TorchKDTree:
                 f"(requested device {device}).")
         if points_ref.shape[0] >= 2 ** 31:
             raise AssertionError("Only 32 bit signed indexing implemented")
-        self.dtype = points_ref.dtype
-        self.dims = points_ref.shape[-1]
-        self.nr_ref_points = points_ref.shape[0]
-        if points_ref.dim() != 2 or self.dtype not in _DTYPES or self.dims not in (1, 2, 3):
+        dtype, dims = points_ref.dtype, points_ref.shape[-1]
+        if points_ref.dim() != 2 or dtype not in _DTYPES or dims not in (1, 2, 3):
             raise RuntimeError(
                 "Could not find the KD-Tree for your specified options. This probably means the library was not "
-                f"compiled for the specified dimensionality ({self.dims}) or precision ({self.dtype}).")
+                f"compiled for the specified dimensionality ({dims}) or precision ({dtype}).")
         if device.index is None:
             device = torch.device("cuda", torch.cuda.current_device())
-        self.device = device
-        self.levels = int(levels)
+        self._setup(points_ref, device, levels, squared_distances, query_opts)
         if build not in ("auto", "host", "device"):
             raise ValueError("build must be 'auto', 'host' or 'device'")
         if build == "auto":
             build = "device" if points_ref.is_cuda else "host"
-        self.built_on = build
         if build == "device":
             pts = points_ref.detach().to(device).contiguous()
             self._tree = _Tree.from_device(pts, self.levels)
         else:
             host = np.ascontiguousarray(points_ref.detach().cpu().numpy())
             self._tree = _Tree(host, self.levels, device.index)
+        self.built_on = build
+
+    def _setup(self, points_ref: torch.Tensor, device: torch.device, levels: int, squared_distances: bool,
+               query_opts: Optional[QueryOpts]) -> None:
+        self.dtype = points_ref.dtype
+        self.dims = points_ref.shape[-1]
+        self.nr_ref_points = points_ref.shape[0]
+        self.device = device
+        self.levels = int(levels)
+        self.built_on = None
         self.dtype_idx = torch.int32
         self.ref_requires_grad = points_ref.requires_grad
         self.points_ref_bak = points_ref
@@ -138,6 +144,22 @@ class TorchKDTree:
         self.query_opts = query_opts
         self._structured = None
         self._shuffled = None
+
+    def save(self, path) -> None:
+        """Write the tree's layout to an ``.npz`` file: the reference's
+        ``structured_points`` and ``shuffled_ind`` plus the split values and
+        leaf offsets.  :func:`load_kd_tree` re-creates the tree from it
+        without rebuilding."""
+        np_dtype = np.float32 if self.dtype == torch.float32 else np.float64
+        med = np.empty((1 << self.levels) - 1, np_dtype)
+        off = np.empty((1 << self.levels) + 1, np.int32)
+        check(LIB.tk_tree_get_splits(self._tree.handle, med.ctypes.data, off.ctypes.data))
+        perm = np.empty(self.nr_ref_points, np.int32)
+        check(LIB.tk_tree_get_perm(self._tree.handle, perm.ctypes.data))
+        pts = np.empty((self.nr_ref_points, self.dims), np_dtype)
+        check(LIB.tk_tree_get_points(self._tree.handle, pts.ctypes.data))
+        np.savez(path, format=np.array(TREE_FORMAT), structured_points=pts, shuffled_ind=perm, split_values=med,
+                 leaf_offsets=off, levels=np.int32(self.levels))
 
     # Layout, as the reference exposes it (torch_kdtree/nn_distance.py:30-41)
     @property
@@ -235,6 +257,47 @@ def build_kd_tree(points_ref: Union[torch.Tensor, np.ndarray], device: Optional[
     return TorchKDTree(points_ref, device, levels, squared_distances, query_opts, build)
 
 
+TREE_FORMAT = "torch_kdtree_gb300.kdtree/1"
+
+
+def load_kd_tree(path, device: Optional[torch.device] = None, squared_distances: bool = True,
+                 query_opts: Optional[QueryOpts] = None) -> TorchKDTree:
+    """Re-create a tree written by :meth:`TorchKDTree.save` on ``device``
+    (default: the current CUDA device) without rebuilding it.  The layout is
+    validated by the library (a corrupt file raises instead of giving inexact
+    answers).  Queries and gradients behave as on the saved tree."""
+    with np.load(path, allow_pickle=False) as z:
+        if str(z["format"]) != TREE_FORMAT:
+            raise ValueError(f"{path} is not a {TREE_FORMAT} file")
+        pts = np.ascontiguousarray(z["structured_points"])
+        perm = np.ascontiguousarray(z["shuffled_ind"], dtype=np.int32)
+        med = np.ascontiguousarray(z["split_values"], dtype=pts.dtype)
+        off = np.ascontiguousarray(z["leaf_offsets"], dtype=np.int32)
+        levels = int(z["levels"])
+    if pts.ndim != 2 or pts.dtype not in (np.float32, np.float64):
+        raise ValueError("structured_points must be [n, dims] float32 or float64")
+    n, d = pts.shape
+    if perm.shape != (n,) or med.shape != ((1 << levels) - 1,) or off.shape != ((1 << levels) + 1,):
+        raise ValueError("layout arrays have inconsistent shapes")
+    device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+    if device.type != "cuda":
+        raise RuntimeError("this engine builds CUDA trees only")
+    if device.index is None:
+        device = torch.device("cuda", torch.cuda.current_device())
+    h = ctypes.c_void_p()
+    check(LIB.tk_tree_create_from_layout(pts.ctypes.data, perm.ctypes.data, med.ctypes.data, off.ctypes.data, n, d,
+                                         _lib.TK_F32 if pts.dtype == np.float32 else _lib.TK_F64, levels,
+                                         device.index, ctypes.byref(h)))
+    orig = np.empty_like(pts)
+    orig[perm] = pts  # the cloud in its original order, for gradients
+    tree = TorchKDTree.__new__(TorchKDTree)
+    tree._setup(torch.from_numpy(orig).to(device), device, levels, squared_distances, query_opts)
+    tree._tree = _Tree(None, levels, device.index)
+    tree._tree.handle = h
+    tree.built_on = "file"
+    return tree
+
+
 _BRUTE_MODES = {"exact": _lib.TK_BRUTE_EXACT, "fp32": _lib.TK_BRUTE_EXACT, "fp64": _lib.TK_BRUTE_EXACT,
                 "tf32": _lib.TK_BRUTE_TF32, "bf16_split": _lib.TK_BRUTE_BF16_SPLIT}
 
@@ -286,3 +349,18 @@ def nn_distance(points_ref: torch.Tensor, points_query: torch.Tensor, nr_nns_sea
     idx = torch.empty((nq, k), dtype=torch.int32, device=ref_c.device)
     nn_distance_raw(ref_c.detach(), q_c.detach(), k, dists, idx, mode)
     return dists, idx
+
+
+def nn_distance_bidirectional(xyz1: torch.Tensor, xyz2: torch.Tensor, nr_nns_searches: int = 1,
+                              mode: str = "exact"):
+    """Both directions of the exhaustive search, as the chamfer-style
+    NmDistance op computes them: ``(dist1, idx1, dist2, idx2)`` with
+    ``dist1, idx1`` the neighbours of every point of ``xyz1`` among ``xyz2``
+    and ``dist2, idx2`` those of ``xyz2`` among ``xyz1``.  The reference's
+    launcher has the second direction commented out
+    (src/nndistance_g.cu:168,219).  Exact and differentiable like
+    :func:`nn_distance`; the two searches run back to back on the current
+    stream."""
+    dist1, idx1 = nn_distance(xyz2, xyz1, nr_nns_searches, mode)
+    dist2, idx2 = nn_distance(xyz1, xyz2, nr_nns_searches, mode)
+    return dist1, idx1, dist2, idx2
