@@ -96,9 +96,7 @@ struct TreeView {
 // never exceeds sqdist(q, p) for a point p in the box; an empty box
 // (lo = +inf, hi = -inf) gives +inf.
 template <typename T, int D>
-__device__ __forceinline__ T box_bound(const PointRec<T>* boxes, int node, const T (&q)[D]) {
-    const PointRec<T> lo = load_rec(boxes + 2 * node);
-    const PointRec<T> hi = load_rec(boxes + 2 * node + 1);
+__device__ __forceinline__ T box_bound_of(const PointRec<T>& lo, const PointRec<T>& hi, const T (&q)[D]) {
     const T l[3] = {lo.x, lo.y, lo.z};
     const T h[3] = {hi.x, hi.y, hi.z};
     T e[D];
@@ -111,6 +109,11 @@ __device__ __forceinline__ T box_bound(const PointRec<T>* boxes, int node, const
     if (D > 1) b = add_rn(b, e[1]);
     if (D > 2) b = add_rn(b, e[2]);
     return b;
+}
+
+template <typename T, int D>
+__device__ __forceinline__ T box_bound(const PointRec<T>* boxes, int node, const T (&q)[D]) {
+    return box_bound_of<T, D>(load_rec(boxes + 2 * node), load_rec(boxes + 2 * node + 1), q);
 }
 
 // Sort R keys ascending in registers (bitonic network, R a power of two).
@@ -174,10 +177,20 @@ __device__ __forceinline__ void kd_search(const TreeView<T>& tv, const T (&q)[D]
             ax = (ax + 1 == D) ? 0 : ax + 1;
         }
         // scan the leaf bucket, G points at a time (unless its box is out of reach)
-        if (!tv.boxes || box_bound<T, D>(tv.boxes, node, q) <= worst_d) {
-            const int leaf = node - first_leaf;
-            int beg = __ldg(tv.leaf_off + leaf);
-            const int end = __ldg(tv.leaf_off + leaf + 1);
+        // (a leaf's box records carry its point range: one round trip for both)
+        int beg, end;
+        bool scan = true;
+        if (tv.boxes) {
+            const PointRec<T> lo = load_rec(tv.boxes + 2 * node);
+            const PointRec<T> hi = load_rec(tv.boxes + 2 * node + 1);
+            scan = box_bound_of<T, D>(lo, hi, q) <= worst_d;
+            beg = int(rec_index(lo));
+            end = int(rec_index(hi));
+        } else {
+            beg = __ldg(tv.leaf_off + (node - first_leaf));
+            end = __ldg(tv.leaf_off + (node - first_leaf) + 1);
+        }
+        if (scan) {
             if (G == 1 && home && k == R && end - beg >= R) {
                 // fill the whole list from the home cell with one sorting
                 // network instead of R single insertions

@@ -208,6 +208,18 @@ int run_query(const tk_tree* t, const T* q, int nq, int k, T* dists, int32_t* id
     return rc;
 }
 
+// The 4th slot of a point record holds an index as raw bits: the original
+// index of a point, or the begin / end offset of a leaf in its box records.
+template <typename T>
+void set_rec_index(PointRec<T>& r, uint32_t v) {
+    if (sizeof(T) == 4) {
+        std::memcpy(&r.w, &v, 4);
+    } else {
+        const uint64_t bits = v;
+        std::memcpy(&r.w, &bits, 8);
+    }
+}
+
 template <typename T>
 int upload_tree(tk_tree* t, const HostTree<T>& h) {
     const int64_t n = h.n;
@@ -218,22 +230,21 @@ int upload_tree(tk_tree* t, const HostTree<T>& h) {
         recs[i].x = c[0];
         recs[i].y = c[1];
         recs[i].z = c[2];
-        if (sizeof(T) == 4) {
-            uint32_t bits = uint32_t(h.perm[i]);
-            std::memcpy(&recs[i].w, &bits, 4);
-        } else {
-            uint64_t bits = uint64_t(uint32_t(h.perm[i]));
-            std::memcpy(&recs[i].w, &bits, 8);
-        }
+        set_rec_index(recs[i], uint32_t(h.perm[i]));
     }
     const size_t b_pts = sizeof(PointRec<T>) * size_t(n);
     const size_t b_med = sizeof(T) * h.medians.size();
     const size_t b_off = sizeof(int32_t) * h.leaf_off.size();
     const size_t nnodes = h.box_lo.size() / 3;
     std::vector<PointRec<T>> boxes(2 * nnodes);
+    const size_t first_leaf = nnodes / 2;  // nnodes = 2^(L+1) - 1
     for (size_t i = 0; i < nnodes; ++i) {
         boxes[2 * i] = PointRec<T>{h.box_lo[3 * i], h.box_lo[3 * i + 1], h.box_lo[3 * i + 2], T(0)};
         boxes[2 * i + 1] = PointRec<T>{h.box_hi[3 * i], h.box_hi[3 * i + 1], h.box_hi[3 * i + 2], T(0)};
+        if (i >= first_leaf) {  // a leaf's box also carries its point range [begin, end)
+            set_rec_index(boxes[2 * i], uint32_t(h.leaf_off[i - first_leaf]));
+            set_rec_index(boxes[2 * i + 1], uint32_t(h.leaf_off[i - first_leaf + 1]));
+        }
     }
     const size_t b_box = sizeof(PointRec<T>) * boxes.size();
     cudaError_t e = cudaMalloc(&t->d_pts, b_pts);

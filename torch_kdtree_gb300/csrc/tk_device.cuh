@@ -20,7 +20,7 @@ namespace tk {
 
 template <typename T>
 struct alignas(4 * sizeof(T)) PointRec {
-    T x, y, z, w;  // w holds the original index as raw bits
+    T x, y, z, w;  // w: raw bits of the original index (of a leaf range bound in box records)
 };
 
 __device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, b); }

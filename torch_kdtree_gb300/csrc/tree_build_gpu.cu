@@ -169,7 +169,8 @@ __global__ void k_make_records(const T* __restrict__ pts, int dims, const uint32
     recs[p] = r;
 }
 
-// Box of every leaf (one warp per leaf), stored at node 2^L - 1 + leaf.
+// Box of every leaf (one warp per leaf), stored at node 2^L - 1 + leaf, with
+// the leaf's point range in the records' 4th slots.
 template <typename T>
 __global__ void k_leaf_boxes(const PointRec<T>* __restrict__ recs, const int32_t* __restrict__ leaf_off,
                              int64_t nleaves, PointRec<T>* __restrict__ boxes) {
@@ -197,10 +198,18 @@ __global__ void k_leaf_boxes(const PointRec<T>* __restrict__ recs, const int32_t
             hi[d] = hi[d] < h ? h : hi[d];
         }
     }
-    if (lane == 0) {
+    if (lane == 0) {  // the box records also carry the leaf's point range [begin, end)
         const int64_t node = nleaves - 1 + leaf;
-        boxes[2 * node] = PointRec<T>{lo[0], lo[1], lo[2], T(0)};
-        boxes[2 * node + 1] = PointRec<T>{hi[0], hi[1], hi[2], T(0)};
+        PointRec<T> a{lo[0], lo[1], lo[2], T(0)}, b{hi[0], hi[1], hi[2], T(0)};
+        if constexpr (sizeof(T) == 4) {
+            a.w = __uint_as_float(uint32_t(leaf_off[leaf]));
+            b.w = __uint_as_float(uint32_t(leaf_off[leaf + 1]));
+        } else {
+            a.w = __longlong_as_double((long long)uint32_t(leaf_off[leaf]));
+            b.w = __longlong_as_double((long long)uint32_t(leaf_off[leaf + 1]));
+        }
+        boxes[2 * node] = a;
+        boxes[2 * node + 1] = b;
     }
 }
 
