@@ -48,12 +48,18 @@ struct BrutePlan {
     int DP, G, R, nsplit, qtiles;
 };
 
-BrutePlan plan_brute(int64_t n, int64_t nq, int d, int k) {
+BrutePlan plan_brute(int64_t n, int64_t nq, int d, int k, bool f32) {
     BrutePlan p;
     p.DP = padded_dims(d);
-    p.G = std::max(1, pow2_ceil((k + 15) / 16));
-    p.R = pow2_ceil((k + p.G - 1) / p.G);
-    if (p.G == 1) p.R = p.R <= 1 ? 1 : (p.R <= 4 ? 4 : 16);
+    if (f32 && p.DP % 4 == 0 && p.DP <= 32 && k <= 32) {
+        // one lane per query with broadcast 16-byte row loads (brute.cuh)
+        p.G = 1;
+        p.R = k <= 1 ? 1 : (k <= 4 ? 4 : (k <= 16 ? 16 : 32));
+    } else {
+        p.G = std::max(1, pow2_ceil((k + 15) / 16));
+        p.R = pow2_ceil((k + p.G - 1) / p.G);
+        if (p.G == 1) p.R = p.R <= 1 ? 1 : (p.R <= 4 ? 4 : 16);
+    }
     const int per_block = 256 / p.G;
     p.qtiles = int((nq + per_block - 1) / per_block);
     const int target = 8 * sm_count_dev();
@@ -80,6 +86,9 @@ int launch_dp(const BruteArgs<T>& a, const BrutePlan& p, cudaStream_t s) {
         done = true;                                                         \
     }
     TK_BR(1, 1) TK_BR(1, 4) TK_BR(1, 16) TK_BR(2, 16) TK_BR(4, 16) TK_BR(8, 16)
+    if constexpr (sizeof(T) == 4 && DP % 4 == 0 && DP <= 32) {
+        TK_BR(1, 32)
+    }
 #undef TK_BR
     if (!done) return fail(TK_EUNSUPPORTED, "no brute-force kernel for this k");
     const cudaError_t e = cudaGetLastError();
@@ -90,7 +99,7 @@ int launch_dp(const BruteArgs<T>& a, const BrutePlan& p, cudaStream_t s) {
 template <typename T>
 int run_brute(const T* ref, int64_t n, const T* q, int64_t nq, int d, int k, T* dists, int32_t* idx, void* ws,
               size_t ws_bytes, cudaStream_t s) {
-    const BrutePlan p = plan_brute(n, nq, d, k);
+    const BrutePlan p = plan_brute(n, nq, d, k, sizeof(T) == 4);
     if (ws_bytes < brute_ws_bytes<T>(p, nq, k) || (p.nsplit > 1 && !ws))
         return fail(TK_EWORKSPACE, "workspace too small");
     BruteArgs<T> a;
@@ -143,14 +152,14 @@ int check_common(const void* ref, int64_t n, const void* q, int64_t nq, int d, i
 // (as planned for 1,024 queries) and launches for the worst case of all nq;
 // blocks past the device-side count exit at once.
 size_t brute_fallback_workspace_bytes(int64_t n, int64_t nq, int d, int k) {
-    BrutePlan p = plan_brute(n, std::min<int64_t>(std::max<int64_t>(nq, 1), 1024), d, k);
+    BrutePlan p = plan_brute(n, std::min<int64_t>(std::max<int64_t>(nq, 1), 1024), d, k, true);
     if (p.nsplit <= 1) return 256;
     return align256(sizeof(Key<float>) * size_t(std::max<int64_t>(nq, 1)) * p.nsplit * k);
 }
 
 int brute_fallback(const float* ref, int64_t n, const float* q, int64_t nq, int d, int k, float* dists,
                    int32_t* idx, const int* qlist, const int* qcount, void* ws, size_t ws_bytes, cudaStream_t s) {
-    BrutePlan p = plan_brute(n, std::min<int64_t>(std::max<int64_t>(nq, 1), 1024), d, k);
+    BrutePlan p = plan_brute(n, std::min<int64_t>(std::max<int64_t>(nq, 1), 1024), d, k, true);
     const int per_block = 256 / p.G;
     p.qtiles = int((nq + per_block - 1) / per_block);
     if (ws_bytes < brute_fallback_workspace_bytes(n, nq, d, k)) return fail(TK_EWORKSPACE, "fallback workspace");
@@ -189,7 +198,7 @@ extern "C" {
 size_t tk_nn_distance_workspace_size(int64_t n, int64_t nq, int dims, int k, int dtype, int mode) {
     if (n < 1 || nq < 0 || k < 1 || dims < 1) return 0;
     if (mode == TK_BRUTE_TF32 || mode == TK_BRUTE_BF16_SPLIT) return brute_tc_workspace_bytes(n, nq, dims, k, mode);
-    const BrutePlan p = plan_brute(n, std::max<int64_t>(nq, 1), dims, k);
+    const BrutePlan p = plan_brute(n, std::max<int64_t>(nq, 1), dims, k, dtype != TK_F64);
     return dtype == TK_F64 ? brute_ws_bytes<double>(p, std::max<int64_t>(nq, 1), k)
                            : brute_ws_bytes<float>(p, std::max<int64_t>(nq, 1), k);
 }

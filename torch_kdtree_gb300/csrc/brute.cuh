@@ -89,7 +89,49 @@ __global__ void __launch_bounds__(256) k_brute(const BruteArgs<T> a) {
             tile[e] = (j < len && c < a.d) ? a.ref[(long long)(t0 + j) * a.d + c] : T(0);
         }
         __syncthreads();
-        if (active) {
+        if constexpr (G == 1 && DP % 4 == 0 && sizeof(T) == 4) {
+            // One lane per query: every lane reads the same reference row, so
+            // a 16-byte shared load broadcasts four coordinates to the warp;
+            // four references per step give four independent chains.  Same
+            // accumulation order as sqdist (dimension by dimension).
+            constexpr int U = 4;
+            static_assert(TR % U == 0, "tile rows must be a multiple of the step");
+            if (active) {
+                const float4* rows = reinterpret_cast<const float4*>(tile);
+                for (int j0 = 0; j0 < len; j0 += U) {
+                    T acc[U];
+#pragma unroll
+                    for (int u = 0; u < U; ++u) {
+                        const float4 v = rows[(j0 + u) * (DP / 4)];
+                        const T d0 = sub_rn(q[0], v.x), d1 = sub_rn(q[1], v.y);
+                        const T d2 = sub_rn(q[2], v.z), d3 = sub_rn(q[3], v.w);
+                        acc[u] = mul_rn(d0, d0);
+                        acc[u] = add_rn(acc[u], mul_rn(d1, d1));
+                        acc[u] = add_rn(acc[u], mul_rn(d2, d2));
+                        acc[u] = add_rn(acc[u], mul_rn(d3, d3));
+                    }
+#pragma unroll
+                    for (int c4 = 1; c4 < DP / 4; ++c4) {
+#pragma unroll
+                        for (int u = 0; u < U; ++u) {
+                            const float4 v = rows[(j0 + u) * (DP / 4) + c4];
+                            const T d0 = sub_rn(q[4 * c4], v.x), d1 = sub_rn(q[4 * c4 + 1], v.y);
+                            const T d2 = sub_rn(q[4 * c4 + 2], v.z), d3 = sub_rn(q[4 * c4 + 3], v.w);
+                            acc[u] = add_rn(acc[u], mul_rn(d0, d0));
+                            acc[u] = add_rn(acc[u], mul_rn(d1, d1));
+                            acc[u] = add_rn(acc[u], mul_rn(d2, d2));
+                            acc[u] = add_rn(acc[u], mul_rn(d3, d3));
+                        }
+                    }
+#pragma unroll
+                    for (int u = 0; u < U; ++u) {
+                        Key<T> mine = Key<T>::sentinel();
+                        if (j0 + u < len) mine = Key<T>::make(acc[u], uint32_t(t0 + j0 + u));
+                        worst = offer<T, G, R>(list, mine, worst, gmask, gl, gbase);
+                    }
+                }
+            }
+        } else if (active) {
             // four references per lane step: four independent accumulation chains
             constexpr int U = DP <= 4 ? 1 : ((DP > 32 || R >= 16) ? 2 : 4);
             for (int j0 = 0; j0 < len; j0 += G * U) {

@@ -135,10 +135,11 @@ struct TopK {
 
     // Insert c (the same value on every lane of the group).  gmask: the
     // group's lanes; gl: this lane's rank in the group.
+    // Slots are rewritten from the top down, so every step still reads the
+    // old values of slot r and r - 1 and no second copy of the list is live.
     __device__ __forceinline__ void insert(const Key<T>& c, unsigned gmask, int gl) {
-        Key<T> nw[R];
 #pragma unroll
-        for (int r = 0; r < R; ++r) {
+        for (int r = R - 1; r >= 0; --r) {
             const Key<T> old = slot[r];
             Key<T> prev;
             bool has_prev;
@@ -153,10 +154,8 @@ struct TopK {
             }
             const bool keep = old.le(c);
             const bool take = !has_prev || prev.le(c);
-            nw[r] = keep ? old : (take ? c : prev);
+            slot[r] = keep ? old : (take ? c : prev);
         }
-#pragma unroll
-        for (int r = 0; r < R; ++r) slot[r] = nw[r];
     }
 
     __device__ __forceinline__ Key<T> worst(unsigned gmask) const {
