@@ -257,8 +257,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc_select(const TcArgs a) {
 constexpr int kT5Rows = 128;   // M (queries per block)
 constexpr int kT5Cols = 256;   // N (references per tile)
 constexpr int kT5EpiWarps = 16; // 4 per 32-lane quarter of the accumulator when reading tensor memory
-constexpr int kT5Chunk = 64;    // accumulator columns moved to shared memory per step
-constexpr int kT5TStride = kT5Chunk + 4;  // transposed tile row stride (floats), bank-conflict free
+constexpr int kT5Chunk = 64;    // accumulator columns per phase (16 per column-group warp)
+constexpr int kT5Buf = 64;      // hit buffer per row: one phase's worth of columns
+constexpr int kT5BufStride = kT5Buf + 1;  // row stride of the hit buffer (keys), spreads rows over banks
 constexpr int kT5Threads = 32 * (kT5EpiWarps + 1);
 constexpr float kT5PadNorm = 1e30f;
 constexpr uint32_t kT5MaxTries = 1u << 22;  // bounded mbarrier polls
@@ -362,9 +363,10 @@ struct Tc5Shape {
     static constexpr uint32_t B_BYTES = uint32_t(kT5Cols) * KB;
     static constexpr int KSTEPS = KB / 32;
     static constexpr size_t SMEM = size_t(PL) * A_BYTES + 2 * size_t(PL) * B_BYTES +
-                                   2 * size_t(kT5Rows) * kT5TStride * sizeof(float) +  // transposed scores
-                                   size_t(kT5Rows) * sizeof(float) +                  // row thresholds
-                                   2 * size_t(kT5Rows) * 4;                           // hit bytes per column group
+                                   size_t(kT5Rows) * kT5BufStride * 8 +  // hit buffer (score keys)
+                                   size_t(kT5Rows) * sizeof(float) +     // row thresholds
+                                   size_t(kT5Rows) * sizeof(int) +       // hit counts
+                                   4 * sizeof(int);                      // overflow / abort flags per tile parity
 };
 
 template <int MODE, int KP, int CH>
@@ -380,9 +382,10 @@ __global__ void __launch_bounds__(kT5Threads, 1) k_tc5_select(const Tc5Args a) {
     extern __shared__ __align__(1024) unsigned char smem[];
     unsigned char* sA = smem;                       // [PL][A_BYTES]
     unsigned char* sB = smem + PL * A_BYTES;        // [2 stages][PL][B_BYTES]
-    float* sT = reinterpret_cast<float*>(sB + 2 * PL * B_BYTES);  // [2][kT5Rows][kT5TStride] transposed scores
-    float* sThr = sT + 2 * kT5Rows * kT5TStride;                     // [kT5Rows] current list threshold per row
-    uint32_t* sHit = reinterpret_cast<uint32_t*>(sThr + kT5Rows);    // [2][kT5Rows] one byte per column group
+    unsigned long long* sBuf = reinterpret_cast<unsigned long long*>(sB + 2 * PL * B_BYTES);  // [kT5Rows][stride]
+    float* sThr = reinterpret_cast<float*>(sBuf + kT5Rows * kT5BufStride);  // [kT5Rows] list threshold per row
+    int* sCnt = reinterpret_cast<int*>(sThr + kT5Rows);                    // [kT5Rows] buffered hits per row
+    int* sFlag = sCnt + kT5Rows;  // [0..1] overflow, [2..3] abort, by tile parity
     __shared__ __align__(8) uint64_t full_a, full_b[2], mma_done[2], epi_done[2];
     __shared__ uint32_t tmem_base_sh;
     __shared__ int abort_sh;
@@ -474,13 +477,19 @@ __global__ void __launch_bounds__(kT5Threads, 1) k_tc5_select(const Tc5Args a) {
         __syncwarp();
     } else {
         // ------------------------------------------------------- epilogue warps
-        // Step A (all 16 warps): warp w copies its 32 accumulator lanes
-        // (quarter w & 3) x 16 columns (group w >> 2) of a 64-column chunk
-        // from tensor memory to the transposed tile sT[row][col].
-        // Step B: warp w owns rows 8w .. 8w+7 and scans them 32 columns per
-        // instruction: one compare, a ballot, and the rare candidates go into
-        // the row's list one at a time, all lanes in step.
+        // Thread (warp w, lane l) reads accumulator lane 32 (w & 3) + l, i.e.
+        // query row `myrow`, and the 16-column group w >> 2 of every 64-column
+        // phase.  Each score is compared with the row's threshold (the worst
+        // key of its over-fetch list, possibly stale but never too small);
+        // the rare hits are appended to the row's buffer in shared memory.
+        // After a tile, warp w merges the buffers of rows 8w .. 8w+7 into
+        // their lists (kept in its registers) and publishes the new
+        // thresholds.  A row can take at most kT5Buf hits per tile on this
+        // path; a tile that overflows a buffer (the first tiles of a slice,
+        // while the lists fill) is done again from tensor memory in four
+        // phases of 64 columns, merging after each, which cannot overflow.
         const int quarter = warp & 3, cgroup = warp >> 2;
+        const int myrow = 32 * quarter + lane;
         RowList<R> lists[ROWS_PER_WARP];
         unsigned long long worst[ROWS_PER_WARP];
 #pragma unroll
@@ -489,89 +498,111 @@ __global__ void __launch_bounds__(kT5Threads, 1) k_tc5_select(const Tc5Args a) {
             worst[i] = kScoreSentinel;
         }
         const uint32_t trow = tmem + (uint32_t(32 * quarter) << 16);
-        constexpr int NCHUNK = kT5Cols / kT5Chunk;
-        if (tid < kT5Rows) sThr[tid] = __int_as_float(0x7f800000);
-        asm volatile("bar.sync 1, %0;" ::"r"(NEPI) : "memory");
-        int step = 0;  // chunk counter over all tiles (selects the sT buffer)
-        bool pending = false;  // step B of the previous chunk still to do
-        int prev_base = 0;
-        auto scan_chunk = [&](int buf, int col_base) {
-            const float* T = sT + buf * kT5Rows * kT5TStride;
+        constexpr int NPHASE = kT5Cols / kT5Chunk;
+        if (tid < kT5Rows) {
+            sThr[tid] = __int_as_float(0x7f800000);
+            sCnt[tid] = 0;
+        }
+        if (tid < 4) sFlag[tid] = 0;
+        auto bar_epi = [&]() { asm volatile("bar.sync 1, %0;" ::"r"(NEPI) : "memory"); };
+        bar_epi();
+        unsigned long long* myBuf = sBuf + myrow * kT5BufStride;
+        // compare 16 scores of columns col0 .. col0+15 with thr, append the hits
+        auto append16 = [&](const float (&v)[16], int col0, float thr, int* ovf) {
+#pragma unroll
+            for (int i = 0; i < 16; ++i) {
+                if (v[i] <= thr && col0 + i < r1) {
+                    const int pos = atomicAdd(&sCnt[myrow], 1);
+                    if (pos < kT5Buf) myBuf[pos] = score_key(v[i], uint32_t(col0 + i));
+                    else *ovf = 1;
+                }
+            }
+        };
+        // merge the buffered hits of this warp's rows into their lists
+        auto merge = [&]() {
 #pragma unroll
             for (int i = 0; i < ROWS_PER_WARP; ++i) {
                 const int row = warp * ROWS_PER_WARP + i;
-                if (sHit[buf * kT5Rows + row] == 0u) continue;  // no score of this row beat its threshold
-                const float* Tr = T + row * kT5TStride;
-#pragma unroll
-                for (int sl = 0; sl < kT5Chunk; sl += 32) {
-                    const float sc = Tr[sl + lane];
-                    const int ref = col_base + sl + lane;
-                    const float wsc = key_score(worst[i]);
-                    unsigned m = __ballot_sync(0xFFFFFFFFu, sc <= wsc && ref < r1);
+                const int n = min(sCnt[row], kT5Buf);
+                if (n == 0) continue;  // uniform: every lane read the same count
+                const unsigned long long* B = sBuf + row * kT5BufStride;
+                for (int b0 = 0; b0 < n; b0 += 32) {
+                    const unsigned long long key = b0 + lane < n ? B[b0 + lane] : kScoreSentinel;
+                    unsigned m = __ballot_sync(0xFFFFFFFFu, key < worst[i]);
                     while (m) {
                         const int src = __ffs(m) - 1;
                         m &= m - 1;
-                        const unsigned long long key =
-                            __shfl_sync(0xFFFFFFFFu, score_key(sc, uint32_t(ref)), src);
-                        if (key < worst[i]) {
-                            lists[i].insert(key, lane);
+                        const unsigned long long c = __shfl_sync(0xFFFFFFFFu, key, src);
+                        if (c < worst[i]) {
+                            lists[i].insert(c, lane);
                             worst[i] = lists[i].worst();
                         }
                     }
                 }
-                if (lane == 0) sThr[row] = key_score(worst[i]);
+                __syncwarp();
+                if (lane == 0) {
+                    sCnt[row] = 0;
+                    sThr[row] = key_score(worst[i]);
+                }
             }
         };
-        bool ok = true;
-        for (int t = 0; t < ntiles && ok; ++t) {
-            const int st = t & 1;
+        for (int t = 0; t < ntiles; ++t) {
+            const int st = t & 1, par = t & 1;
             const uint32_t ph = (t >> 1) & 1;
+            const int base = r0 + t * kT5Cols;
+            const uint32_t tcol = trow + uint32_t(st * kT5Cols);
             int w_ok = 1;
-            if (lane == 0) w_ok = sm100::mbar_wait(&mma_done[st], ph, kT5MaxTries) && !abort_sh;
+            if (lane == 0) w_ok = sm100::mbar_wait(&mma_done[st], ph, kT5MaxTries);
             w_ok = __shfl_sync(0xFFFFFFFFu, w_ok, 0);
-            if (!w_ok) {
-                if (lane == 0) {
-                    atomicExch(&abort_sh, 1);
-                    atomicExch(a.err, 1);
-                }
-                ok = false;
+            if (tid == 0) {  // flags of the next tile (their last readers passed this tile's first barrier)
+                sFlag[par ^ 1] = 0;
+                sFlag[2 + (par ^ 1)] = 0;
             }
-            // epilogue warps agree on `ok` through the named barrier below
-            for (int ch = 0; ch < NCHUNK; ++ch) {
-                const int buf = step & 1;
-                if (ok) {
-                    sm100::tc_fence_after();
+            if (w_ok) {
+                sm100::tc_fence_after();
+                const float thr = sThr[myrow];
+#pragma unroll
+                for (int j = 0; j < NPHASE; ++j) {
                     float v[16];
-                    sm100::tmem_ld16(trow + uint32_t(st * kT5Cols + ch * kT5Chunk + cgroup * 16), v);
-                    const int myrow = 32 * quarter + lane;
-                    float* dst = sT + buf * kT5Rows * kT5TStride + myrow * kT5TStride + cgroup * 16;
-#pragma unroll
-                    for (int i = 0; i < 16; i += 4)
-                        *reinterpret_cast<float4*>(dst + i) = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
-                    // pre-filter against the row's (possibly stale, never too small) threshold
-                    const float thr = sThr[myrow];
-                    bool hit = false;
-#pragma unroll
-                    for (int i = 0; i < 16; ++i) hit |= v[i] <= thr;
-                    reinterpret_cast<uint8_t*>(sHit + buf * kT5Rows + myrow)[cgroup] = hit ? 1 : 0;
-                    if (ch == NCHUNK - 1) {  // this tile's accumulator is no longer read
-                        sm100::tc_fence_before();
-                        __syncwarp();
-                        if (lane == 0) sm100::mbar_arrive(&epi_done[st]);
+                    sm100::tmem_ld16(tcol + uint32_t(j * kT5Chunk + cgroup * 16), v);
+                    append16(v, base + j * kT5Chunk + cgroup * 16, thr, &sFlag[par]);
+                }
+            } else if (lane == 0) {
+                sFlag[2 + par] = 1;
+            }
+            bar_epi();
+            const int bad = sFlag[2 + par];   // agreed: written only before the barrier above
+            const int ovf = sFlag[par];
+            if (!bad) {
+                if (!ovf) {
+                    merge();
+                } else {
+                    // redo the tile in four phases of 64 columns
+                    if (tid < kT5Rows) sCnt[tid] = 0;
+                    bar_epi();
+#pragma unroll 1
+                    for (int j = 0; j < NPHASE; ++j) {
+                        const float thr = sThr[myrow];
+                        float v[16];
+                        sm100::tmem_ld16(tcol + uint32_t(j * kT5Chunk + cgroup * 16), v);
+                        int dummy = 0;
+                        append16(v, base + j * kT5Chunk + cgroup * 16, thr, &dummy);  // <= 64 hits per row
+                        bar_epi();
+                        merge();
+                        bar_epi();
                     }
                 }
-                // previous chunk's rows while this one lands in the other buffer
-                if (pending) scan_chunk(buf ^ 1, prev_base);
-                asm volatile("bar.sync 1, %0;" ::"r"(NEPI) : "memory");
-                const int bad = abort_sh;
-                if (bad) ok = false;
-                pending = ok;
-                prev_base = r0 + t * kT5Cols + ch * kT5Chunk;
-                ++step;
-                if (!ok) break;
+            }
+            // this tile's accumulator is no longer read
+            sm100::tc_fence_before();
+            __syncwarp();
+            if (lane == 0) sm100::mbar_arrive(&epi_done[st]);
+            bar_epi();
+            if (bad) {
+                if (tid == 0) atomicExch(a.err, 1);
+                break;
             }
         }
-        if (pending) scan_chunk((step - 1) & 1, prev_base);
         // write the lists: C candidates per row and the row threshold
 #pragma unroll
         for (int i = 0; i < ROWS_PER_WARP; ++i) {
