@@ -260,6 +260,7 @@ constexpr int kT5EpiWarps = 16; // 4 per 32-lane quarter of the accumulator when
 constexpr int kT5Chunk = 64;    // accumulator columns per phase (16 per column-group warp)
 constexpr int kT5Buf = 64;      // hit buffer per row: one phase's worth of columns
 constexpr int kT5BufStride = kT5Buf + 1;  // row stride of the hit buffer (keys), spreads rows over banks
+constexpr int kT5BatchMin = 8;  // hits of a row merged as one sorted batch from this many on
 constexpr int kT5Threads = 32 * (kT5EpiWarps + 1);
 constexpr float kT5PadNorm = 1e30f;
 constexpr uint32_t kT5MaxTries = 1u << 22;  // bounded mbarrier polls
@@ -352,6 +353,64 @@ struct RowList {
         for (int r = 0; r < R; ++r) slot[r] = nw[r];
     }
     __device__ __forceinline__ unsigned long long worst() const { return __shfl_sync(0xFFFFFFFFu, slot[R - 1], 31); }
+
+    // Keep the 32 R smallest of the list and the batch x (32 R keys in the
+    // list's layout, any order, sentinel-padded): bitonic sort of x, then
+    // element-wise min of the list and the reversed batch (which holds the
+    // 32 R smallest of both, as a bitonic sequence) and a bitonic clean-up.
+    // The padding slots at the front are zeros and stay there.
+    __device__ __forceinline__ void merge_batch(unsigned long long (&x)[R], int lane) {
+        constexpr int S = 32 * R;
+#pragma unroll
+        for (int size = 2; size <= S; size <<= 1) {
+#pragma unroll
+            for (int stride = size >> 1; stride > 0; stride >>= 1) {
+                if (stride == 32) {  // partner in the same lane, other register (R == 2)
+#pragma unroll
+                    for (int r = 0; r + 1 < R; r += 2) {
+                        const unsigned long long a = x[r], b = x[r + 1];
+                        x[r] = a < b ? a : b;  // size == 64 == S: ascending
+                        x[r + 1] = a < b ? b : a;
+                    }
+                } else {
+#pragma unroll
+                    for (int r = 0; r < R; ++r) {
+                        const unsigned long long p = __shfl_xor_sync(0xFFFFFFFFu, x[r], stride);
+                        const int sidx = r * 32 + lane;
+                        const bool asc = (sidx & size) == 0;
+                        const bool lower = (lane & stride) == 0;
+                        const bool take_min = asc == lower;
+                        const bool p_less = p < x[r];
+                        x[r] = (take_min == p_less) ? p : x[r];
+                    }
+                }
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const unsigned long long b = __shfl_sync(0xFFFFFFFFu, x[R - 1 - r], 31 - lane);
+            slot[r] = b < slot[r] ? b : slot[r];
+        }
+#pragma unroll
+        for (int stride = S >> 1; stride > 0; stride >>= 1) {
+            if (stride == 32) {
+#pragma unroll
+                for (int r = 0; r + 1 < R; r += 2) {
+                    const unsigned long long a = slot[r], b = slot[r + 1];
+                    slot[r] = a < b ? a : b;
+                    slot[r + 1] = a < b ? b : a;
+                }
+            } else {
+#pragma unroll
+                for (int r = 0; r < R; ++r) {
+                    const unsigned long long p = __shfl_xor_sync(0xFFFFFFFFu, slot[r], stride);
+                    const bool lower = (lane & stride) == 0;
+                    const bool p_less = p < slot[r];
+                    slot[r] = (lower == p_less) ? p : slot[r];
+                }
+            }
+        }
+    }
 };
 
 template <int MODE, int KP, int CH>
@@ -526,16 +585,30 @@ __global__ void __launch_bounds__(kT5Threads, 1) k_tc5_select(const Tc5Args a) {
                 const int n = min(sCnt[row], kT5Buf);
                 if (n == 0) continue;  // uniform: every lane read the same count
                 const unsigned long long* B = sBuf + row * kT5BufStride;
-                for (int b0 = 0; b0 < n; b0 += 32) {
-                    const unsigned long long key = b0 + lane < n ? B[b0 + lane] : kScoreSentinel;
-                    unsigned m = __ballot_sync(0xFFFFFFFFu, key < worst[i]);
-                    while (m) {
-                        const int src = __ffs(m) - 1;
-                        m &= m - 1;
-                        const unsigned long long c = __shfl_sync(0xFFFFFFFFu, key, src);
-                        if (c < worst[i]) {
-                            lists[i].insert(c, lane);
-                            worst[i] = lists[i].worst();
+                if (n >= kT5BatchMin) {
+                    // many hits (while the list fills): one sorted merge per 32 R of them
+                    for (int b0 = 0; b0 < n; b0 += 32 * R) {
+                        unsigned long long x[R];
+#pragma unroll
+                        for (int r = 0; r < R; ++r) {
+                            const int e = b0 + r * 32 + lane;
+                            x[r] = e < n ? B[e] : kScoreSentinel;
+                        }
+                        lists[i].merge_batch(x, lane);
+                    }
+                    worst[i] = lists[i].worst();
+                } else {
+                    for (int b0 = 0; b0 < n; b0 += 32) {
+                        const unsigned long long key = b0 + lane < n ? B[b0 + lane] : kScoreSentinel;
+                        unsigned m = __ballot_sync(0xFFFFFFFFu, key < worst[i]);
+                        while (m) {
+                            const int src = __ffs(m) - 1;
+                            m &= m - 1;
+                            const unsigned long long c = __shfl_sync(0xFFFFFFFFu, key, src);
+                            if (c < worst[i]) {
+                                lists[i].insert(c, lane);
+                                worst[i] = lists[i].worst();
+                            }
                         }
                     }
                 }
