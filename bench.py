@@ -629,13 +629,14 @@ def run_brute_tc(args):
     k = 32
     out = {}
     if args.profile:
-        # one tensor-core call on a reduced query set (for ncu captures)
+        # one tensor-core and one exact call on a reduced query set (for ncu captures)
         ref_np, q_np = tensor_core_brute(d=32, n_query=16384)
         ref = torch.from_numpy(ref_np).to(dev)
         q = torch.from_numpy(q_np).to(dev)
         dd = torch.empty(len(q), k, device=dev)
         ii = torch.empty(len(q), k, dtype=torch.int32, device=dev)
         nn_distance_raw(ref, q, k, dd, ii, "tf32")
+        nn_distance_raw(ref, q, k, dd, ii, "exact")
         torch.cuda.synchronize()
         return
     for d in (8, 32):
