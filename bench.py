@@ -333,17 +333,11 @@ def run_ours(args, rank, world):
 
     ms_e2e = timed(step_e2e, args.steps, args.warmup)
 
-    # max over ranks
-    def world_max(v):
-        if world == 1:
-            return v
-        t = torch.tensor([v], dtype=torch.float64, device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        return float(t.item())
-
-    t_chosen = world_max(sum(ms_chosen))
-    t_plain = world_max(sum(ms_plain))
-    t_e2e = world_max(sum(ms_e2e))
+    # max over ranks (the slowest replica sets the job time)
+    from torch_kdtree_gb300.distributed import world_max
+    t_chosen = world_max(sum(ms_chosen), dev)
+    t_plain = world_max(sum(ms_plain), dev)
+    t_e2e = world_max(sum(ms_e2e), dev)
     if rank != 0:
         return
 
