@@ -121,3 +121,23 @@ def test_tensor_core_fallback_on_massive_ties(mode, oracle):
     bd, bi = oracle.brute(ref, q, 20)
     np.testing.assert_array_equal(dd.cpu().numpy(), bd)
     np.testing.assert_array_equal(ii.cpu().numpy(), bi)
+
+
+def test_auto_mode_picks_a_mode_and_stays_exact(tmp_path, monkeypatch, oracle):
+    """mode="auto" times the modes once (cached) and returns the exact answer."""
+    import torch_kdtree_gb300.autotune as at
+    from torch_kdtree_gb300 import nn_distance
+    monkeypatch.setattr(at, "CACHE_PATH", str(tmp_path / "cache.json"))
+    rng = np.random.default_rng(44)
+    for d, dtype in ((32, np.float32), (3, np.float32), (3, np.float64)):
+        ref = rng.standard_normal((20000, d)).astype(dtype)
+        q = rng.standard_normal((700, d)).astype(dtype)
+        rt, qt = torch.from_numpy(ref).to(cuda), torch.from_numpy(q).to(cuda)
+        mode = at.autotune_brute(rt, qt, 8)
+        assert mode in (("exact",) if dtype == np.float64 else ("exact", "tf32", "bf16_split"))
+        dd, ii = nn_distance(rt, qt, 8, mode="auto")
+        bd, bi = oracle.brute(ref, q, 8)
+        np.testing.assert_array_equal(dd.cpu().numpy(), bd)
+        np.testing.assert_array_equal(ii.cpu().numpy(), bi)
+    import json
+    assert len(json.load(open(tmp_path / "cache.json"))) == 3

@@ -126,3 +126,45 @@ def build_tuned_kd_tree(points_ref: torch.Tensor, queries: torch.Tensor, k: int,
     """build_kd_tree with the autotuned depth and launch options."""
     ch = autotune(points_ref, queries, k, **kw)
     return build_kd_tree(points_ref, levels=ch.levels, query_opts=ch.opts())
+
+
+def autotune_brute(points_ref: torch.Tensor, points_query: torch.Tensor, k: int, reps: int = 3,
+                   use_cache: bool = True, max_queries: int = 16384) -> str:
+    """Pick the fastest exhaustive-search mode for these shapes: "exact" (CUDA
+    cores) or, for float32 with d <= 64 and k <= 64, "tf32" / "bf16_split"
+    (tensor-core candidates + exact re-rank).  Every mode returns the same
+    exact answer, so only speed decides.  A sample of at most ``max_queries``
+    queries is timed; choices are cached like the KD launch choices."""
+    from .nn_distance import nn_distance_raw
+    n, d = points_ref.shape
+    key = "brute|" + _key(n, points_query.shape[0], k, d, str(points_ref.dtype), points_ref.device)
+    cache = _load_cache() if use_cache else {}
+    if use_cache and key in cache:
+        return cache[key]["mode"]
+    modes = ["exact"]
+    if points_ref.dtype == torch.float32 and d <= 64 and k <= 64:
+        modes += ["tf32", "bf16_split"]
+    q = points_query[:max_queries].contiguous()
+    ref = points_ref.contiguous()
+    dd = torch.empty(q.shape[0], k, dtype=ref.dtype, device=ref.device)
+    ii = torch.empty(q.shape[0], k, dtype=torch.int32, device=ref.device)
+    best, table = None, []
+    for m in modes:
+        nn_distance_raw(ref, q, k, dd, ii, m)  # warm-up
+        times = []
+        for _ in range(reps):
+            s = torch.cuda.Event(enable_timing=True)
+            e = torch.cuda.Event(enable_timing=True)
+            s.record()
+            nn_distance_raw(ref, q, k, dd, ii, m)
+            e.record()
+            e.synchronize()
+            times.append(s.elapsed_time(e))
+        ms = sorted(times)[len(times) // 2]
+        table.append((m, ms))
+        if best is None or ms < best[1]:
+            best = (m, ms)
+    if use_cache:
+        cache[key] = {"mode": best[0], "table": table}
+        _store_cache(cache)
+    return best[0]

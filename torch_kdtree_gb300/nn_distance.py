@@ -323,11 +323,13 @@ def nn_distance(points_ref: torch.Tensor, points_query: torch.Tensor, nr_nns_sea
 
     ``mode``: "exact" (CUDA cores, float32 or float64), "tf32" or
     "bf16_split" (tensor-core candidate search with an exact float32 re-rank;
-    same answer).  Differentiable in both point sets.  The reference shipped
-    this search as an unbound CUDA launcher (src/nndistance_g.cu:191-220) for
-    d = 3 only; here any 1 <= d <= 128 (float64: d <= 4)."""
-    if mode not in _BRUTE_MODES:
-        raise ValueError(f"mode must be one of {sorted(_BRUTE_MODES)}")
+    same answer), or "auto" (the fastest of these for the shapes, timed once
+    by :func:`torch_kdtree_gb300.autotune.autotune_brute` and cached).
+    Differentiable in both point sets.  The reference shipped this search as
+    an unbound CUDA launcher (src/nndistance_g.cu:191-220) for d = 3 only;
+    here any 1 <= d <= 128 (float64: d <= 4)."""
+    if mode not in _BRUTE_MODES and mode != "auto":
+        raise ValueError(f"mode must be one of {sorted(_BRUTE_MODES) + ['auto']}")
     if points_ref.device.type != "cuda":
         raise RuntimeError("nn_distance runs on CUDA tensors only")
     if points_ref.dtype not in _DTYPES or points_query.dtype != points_ref.dtype:
@@ -338,6 +340,9 @@ def nn_distance(points_ref: torch.Tensor, points_query: torch.Tensor, nr_nns_sea
     if k > points_ref.shape[0]:
         raise RuntimeError("You requested more nearest neighbors than there are reference points")
     points_query = points_query.to(points_ref.device)
+    if mode == "auto":
+        from .autotune import autotune_brute
+        mode = autotune_brute(points_ref.detach(), points_query.detach(), k)
     ref_c = points_ref.contiguous()
     q_c = points_query.contiguous()
     need_grad = torch.is_grad_enabled() and (points_ref.requires_grad or points_query.requires_grad)
