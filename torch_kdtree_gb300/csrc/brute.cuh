@@ -11,7 +11,10 @@
 //   * distances use the reference's CPU arithmetic (sqdist order, no fused
 //     multiply-add), so results match the KD-tree query bit for bit;
 //   * each slice keeps the k best (distance, index) keys in registers (TopK);
-//     with several slices a merge kernel combines the per-slice lists.
+//     with several slices a merge kernel combines the per-slice lists;
+//   * with one lane per query a candidate is first tested as a float against
+//     the list's worst distance (one compare), and only the rare survivors
+//     build and compare the 64-bit (distance, index) key.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -125,9 +128,9 @@ __global__ void __launch_bounds__(256) k_brute(const BruteArgs<T> a) {
                     }
 #pragma unroll
                     for (int u = 0; u < U; ++u) {
-                        Key<T> mine = Key<T>::sentinel();
-                        if (j0 + u < len) mine = Key<T>::make(acc[u], uint32_t(t0 + j0 + u));
-                        worst = offer<T, G, R>(list, mine, worst, gmask, gl, gbase);
+                        if (j0 + u < len && acc[u] <= worst.dist())
+                            worst = offer<T, G, R>(list, Key<T>::make(acc[u], uint32_t(t0 + j0 + u)), worst, gmask,
+                                                   gl, gbase);
                     }
                 }
             }
@@ -155,9 +158,15 @@ __global__ void __launch_bounds__(256) k_brute(const BruteArgs<T> a) {
 #pragma unroll
                 for (int u = 0; u < U; ++u) {
                     const int j = j0 + u * G + gl;
-                    Key<T> mine = Key<T>::sentinel();
-                    if (j < len) mine = Key<T>::make(acc[u], uint32_t(t0 + j));
-                    worst = offer<T, G, R>(list, mine, worst, gmask, gl, gbase);
+                    if constexpr (G == 1) {
+                        if (j < len && acc[u] <= worst.dist())
+                            worst = offer<T, G, R>(list, Key<T>::make(acc[u], uint32_t(t0 + j)), worst, gmask, gl,
+                                                   gbase);
+                    } else {
+                        Key<T> mine = Key<T>::sentinel();
+                        if (j < len) mine = Key<T>::make(acc[u], uint32_t(t0 + j));
+                        worst = offer<T, G, R>(list, mine, worst, gmask, gl, gbase);
+                    }
                 }
             }
         }
