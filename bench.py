@@ -129,15 +129,42 @@ def fp64_error(ref, q, dists, idx, chunk=1 << 18):
     return {"max_rel_err": worst, "queries_with_equal_distances_in_list": ties}
 
 
-def profiled_traffic(kernel_tag: str):
-    """DRAM bytes per launch of a kernel from its committed ncu summary
-    (profiles/<kernel_tag>.md, line 'traffic_bytes_per_launch: <int>'), or None."""
+def profiled_value(kernel_tag: str, field: str = "traffic_bytes_per_launch"):
+    """A per-launch figure of a kernel from its committed ncu summary
+    (profiles/<kernel_tag>.md, line '<field>: <int>'), or None."""
     path = os.path.join(ROOT, "profiles", kernel_tag + ".md")
     try:
-        m = re.search(r"traffic_bytes_per_launch:\s*([0-9]+)", open(path).read())
+        m = re.search(field + r":\s*([0-9]+)", open(path).read())
         return int(m.group(1)) if m else None
     except OSError:
         return None
+
+
+def profiled_traffic(kernel_tag: str):
+    """DRAM bytes (read + write) per launch from the kernel's ncu summary, or None."""
+    return profiled_value(kernel_tag, "traffic_bytes_per_launch")
+
+
+def issue_roofline(kernel_tag: str, kernel_ms: float, dev_index: int):
+    """Instruction-issue roofline of an issue-bound kernel: warp instructions
+    per launch (from its ncu summary) over the measured launch time, against
+    one warp instruction per cycle per scheduler (4 per SM) at the maximum SM
+    clock."""
+    import torch
+    inst = profiled_value(kernel_tag, "warp_instructions_per_launch")
+    if inst is None:
+        return None
+    props = torch.cuda.get_device_properties(dev_index)
+    mhz = 2070.0
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            mhz = float(json.load(f).get("sm_max_mhz", mhz))
+    except (OSError, ValueError):
+        pass
+    peak = props.multi_processor_count * 4 * mhz * 1e6 / 1e9  # G warp instructions / s
+    achieved = inst / (kernel_ms / 1e3) / 1e9
+    return {"achieved": achieved, "peak": peak, "unit": "G warp instructions/s", "frac": achieved / peak,
+            "warp_instructions_per_launch": inst}
 
 
 def algorithmic_bytes(n_ref, nq, k, levels, d=3):
@@ -376,7 +403,8 @@ def run_ours(args, rank, world):
         "autotune_table": [list(map(lambda x: round(x, 4) if isinstance(x, float) else x, r)) for r in ch.table],
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_kind": peak_kind, "traffic": traffic, "kernel": kernel_name,
-                     "kernel_ms": kern_avg, "algorithmic_bytes_per_launch": alg},
+                     "kernel_ms": kern_avg, "algorithmic_bytes_per_launch": alg,
+                     "issue": issue_roofline(kernel_name[2:] + "_cube_sphere_4M_k16", kern_avg, dev.index)},
         "cpu_baseline": cpu,
         "exactness_vs_oracle_sample": exact,
         "fp32_dists_vs_fp64_recomputation": fp64,
