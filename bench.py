@@ -585,6 +585,53 @@ def run_brute(args):
 
 
 
+def run_readme(args):
+    """The reference's own benchmark setting (its README plot): references and
+    queries N(0,1) * 1e3 in 3-D, default tree depth, query() called on a host
+    tensor and followed by a synchronize, timed on the wall clock (as its
+    benchmark script does), here at its largest size, 1e6 x 1e6, for k = 1, 10
+    and 100.  Also reported: the same query with device-resident inputs (CUDA
+    events) and the published RTX 3090 readings of that plot."""
+    import numpy as np
+    import torch
+
+    import torch_kdtree_gb300 as tk
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    rng = np.random.default_rng(0)
+    n = nq = 1_000_000
+    ref = torch.from_numpy((rng.standard_normal((n, 3)) * 1e3).astype(np.float32)).to(dev)
+    q_host = torch.from_numpy((rng.standard_normal((nq, 3)) * 1e3).astype(np.float32))
+    q_dev = q_host.to(dev)
+    tree = tk.build_kd_tree(ref)
+    published = {1: "1e7-3e7", 10: "~1e7", 100: "2e6-4e6"}  # q/s, visual readings of the plot
+    runs = {}
+    for k in (1, 10, 100):
+        def call():
+            tree.query(q_host, nr_nns_searches=k)
+            torch.cuda.synchronize()
+        for _ in range(max(args.warmup, 1)):
+            call()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            call()
+        wall = (time.perf_counter() - t0) / args.steps
+        ms = _event_ms(lambda: tree.query(q_dev, nr_nns_searches=k), args.steps, args.warmup)
+        runs[f"k{k}"] = {"queries_per_s_host_input_wall": nq / wall, "ms_host_input_wall": 1e3 * wall,
+                         "queries_per_s_device_resident": nq / (sum(ms) / len(ms) / 1e3),
+                         "reference_rtx3090_published_queries_per_s": published[k]}
+    line = {
+        "metric": "KNN queries/s, reference benchmark setting (1e6 refs x 1e6 queries N(0,1)*1e3, d=3, default depth)",
+        "value": runs["k10"]["queries_per_s_host_input_wall"], "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": runs["k10"]["ms_host_input_wall"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded numpy)",
+        "config": {"workload": "torch_kdtree benchmark/benchmark.py setting at 1e6 x 1e6; value = k=10",
+                   "levels": tree.levels, "timing": "wall clock around query(host tensor) + synchronize"},
+        "runs": runs,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_plain(args):
     """Plain KD-tree KNN: 100,000 refs and 10,000 queries N(0,1)*1e3, k=5, the
     reference's default depth; GPU query (graph-replayed, inputs resident) vs
@@ -709,7 +756,8 @@ def main():
     p.add_argument("--traversal", type=int, default=1, choices=[1, 2],
                    help="chosen: 1 = per-query stacks, 2 = warp packets (with --levels/--tpq)")
     p.add_argument("--profile", action="store_true", help="run one chosen and one plain query only (for ncu)")
-    p.add_argument("--workload", default="kd", choices=["kd", "plain", "batched", "backward", "brute", "brute_tc"],
+    p.add_argument("--workload", default="kd",
+                   choices=["kd", "plain", "readme", "batched", "backward", "brute", "brute_tc"],
                    help="kd (default): the headline large single-cloud query; the others measure the "
                         "batched, backward and brute-force paths")
     p.add_argument("--leaf-size", type=int, default=16, help="target points per leaf of tuned batch trees")
@@ -723,7 +771,8 @@ def main():
         return
     if args.workload != "kd":
         if rank == 0:
-            {"plain": run_plain, "batched": run_batched, "backward": run_backward, "brute": run_brute,
+            {"plain": run_plain, "readme": run_readme, "batched": run_batched, "backward": run_backward,
+             "brute": run_brute,
              "brute_tc": run_brute_tc}[args.workload](args)
         return
     if world > 1:
