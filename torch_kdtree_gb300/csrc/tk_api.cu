@@ -103,13 +103,16 @@ bool gr_available(int dtype, int dims, int G, int R) {
     return true;
 }
 
-// Lanes per query when the caller leaves it open: enough lanes to share a
-// leaf's points (about 12-24 points per lane), and, for small query counts,
-// enough to give every SM about 1024 threads (10,000 queries on one lane each
-// fill only 40 of 152 SMs; 16 lanes each ran 1.6x faster).
-int auto_lanes(const tk_tree* t, int64_t nq) {
+// Lanes per query when the caller leaves it open (measured on 1M-query
+// workloads): one lane per query up to ~192 points per leaf and k <= 16 (its
+// list fits one lane's registers); 32 lanes for larger leaves or k > 16,
+// which spread both the leaf scan and the list (k = 100: 21 ms on 32 lanes,
+// 35 ms on 8).  For small query counts, enough lanes to give every SM about
+// 1024 threads (10,000 queries on one lane each fill only 40 of 152 SMs; 16
+// lanes each ran 1.6x faster).
+int auto_lanes(const tk_tree* t, int64_t nq, int k) {
     const double avg_leaf = double(t->n) / double(int64_t(1) << t->levels);
-    int g = avg_leaf <= 24 ? 1 : avg_leaf <= 48 ? 2 : avg_leaf <= 96 ? 4 : avg_leaf <= 192 ? 8 : avg_leaf <= 384 ? 16 : 32;
+    int g = (k > 16 || avg_leaf > 192) ? 32 : 1;
     const int64_t target = int64_t(sm_count(t->device)) * 1024;
     while (g < 32 && nq * g < target) g <<= 1;
     return g;
@@ -130,7 +133,7 @@ int run_query(const tk_tree* t, const T* q, int nq, int k, T* dists, int32_t* id
     // lanes per query and registers per lane
     int G = 1, R = pow2_ceil(k);
     if (!packet) {
-        G = o.threads_per_query > 0 ? o.threads_per_query : auto_lanes(t, nq);
+        G = o.threads_per_query > 0 ? o.threads_per_query : auto_lanes(t, nq, k);
         if (G != 1 && G != 2 && G != 4 && G != 8 && G != 16 && G != 32)
             return fail(TK_EINVAL, "threads_per_query must be 1, 2, 4, 8, 16 or 32");
         G = std::max(G, pow2_ceil((k + 15) / 16));
