@@ -158,6 +158,51 @@ struct TopK {
         }
     }
 
+    // G == 32: merge one candidate per lane (sentinel where none) at once:
+    // bitonic sort of the 32 candidates across the warp, element-wise min of
+    // the list's last 32 slots with the reversed sorted batch (the list and the
+    // batch, padded with sentinels to the list's length, give a bitonic
+    // sequence holding the 32 R smallest of both), then a bitonic clean-up.
+    // Same result as inserting the candidates one by one.
+    __device__ __forceinline__ void merge_warp_batch(Key<T> x, int lane) {
+        static_assert(G == 32, "one candidate per lane of a full warp");
+#pragma unroll
+        for (int size = 2; size <= 32; size <<= 1) {
+#pragma unroll
+            for (int stride = size >> 1; stride > 0; stride >>= 1) {
+                const Key<T> p = x.shfl(0xFFFFFFFFu, lane ^ stride, 32);
+                const bool take_min = ((lane & size) == 0) == ((lane & stride) == 0);
+                const bool p_less = p.lt(x);
+                x = (take_min == p_less) ? p : x;
+            }
+        }
+        const Key<T> b = x.shfl(0xFFFFFFFFu, 31 - lane, 32);
+        slot[R - 1] = b.lt(slot[R - 1]) ? b : slot[R - 1];
+#pragma unroll
+        for (int stride = 16 * R; stride > 0; stride >>= 1) {
+            if (stride >= 32) {
+                const int rs = stride / 32;
+#pragma unroll
+                for (int r = 0; r < R; ++r) {
+                    if ((r & rs) == 0) {
+                        const Key<T> a = slot[r], c = slot[r + rs];
+                        const bool sw = c.lt(a);
+                        slot[r] = sw ? c : a;
+                        slot[r + rs] = sw ? a : c;
+                    }
+                }
+            } else {
+#pragma unroll
+                for (int r = 0; r < R; ++r) {
+                    const Key<T> p = slot[r].shfl(0xFFFFFFFFu, lane ^ stride, 32);
+                    const bool lower = (lane & stride) == 0;
+                    const bool p_less = p.lt(slot[r]);
+                    slot[r] = (lower == p_less) ? p : slot[r];
+                }
+            }
+        }
+    }
+
     __device__ __forceinline__ Key<T> worst(unsigned gmask) const {
         if (G == 1) return slot[R - 1];
         return slot[R - 1].shfl(gmask, G - 1, G);
@@ -191,6 +236,12 @@ __device__ __forceinline__ Key<T> offer(TopK<T, G, R>& list, const Key<T>& mine,
     }
     unsigned m = __ballot_sync(gmask, mine.lt(worst));
     if constexpr (G < 32) m = (m >> gbase) & ((1u << G) - 1u);
+    if constexpr (G == 32) {
+        if (__popc(m) >= 8) {  // many at once (while the list fills): one sorted merge
+            list.merge_warp_batch(mine.lt(worst) ? mine : Key<T>::sentinel(), gl);
+            return list.worst(gmask);
+        }
+    }
     while (m) {
         const int src = __ffs(m) - 1;
         m &= m - 1;
