@@ -26,7 +26,7 @@
 #include <stdlib.h>
 #include <string.h>
 
-#define ORC_TREE_MAX_D 3
+#define ORC_TREE_MAX_D 8
 #define ORC_MAX_D 128
 
 enum { TAG_NONE = 0, TAG_LEFT = 1, TAG_RIGHT = 2, TAG_BOTH = 3 };

@@ -1,8 +1,9 @@
 // ORACLE (test infrastructure): a C-ABI wrapper of our own around the
 // reference's CPU KD-tree (createKDTree, src/kdtree.hpp:494-534, and
-// KDTreeKNNSearch, src/kdtree.cpp:164-194), compiled together with the
-// reference's unmodified src/kdtree.cpp by `make -C oracle ref`.  It plays
-// the part of the reference's pybind class KDTreeCPU{1,2,3}D[F]
+// KDTreeKNNSearch, src/kdtree.cpp:164-194), compiled with the reference's
+// unmodified src/kdtree.cpp (included below) by `make -C oracle ref`.  It plays
+// the part of the reference's pybind class KDTreeCPU{1,2,3}D[F] (and of the
+// classes its README's recipe adds for more dimensions)
 // (src/interface.cpp:13-95): build on the host, expose the layout getters,
 // query with raw pointers.  Used by tests/golden/make_golden.py to produce
 // fixtures and, where it was built, as the timed CPU baseline.
@@ -11,7 +12,12 @@
 #include <stdexcept>
 #include <string>
 
-#include "kdtree.hpp"
+// The reference's src/kdtree.cpp, unmodified, compiled in this translation
+// unit: its KD-tree search and PartitionInfo are templates defined there, and
+// seeing the definitions lets this wrapper instantiate them for 4-8 dimensions
+// too (the reference's README recipe for more dimensions is to add such
+// instantiations).
+#include "kdtree.cpp"
 
 namespace {
 
@@ -55,17 +61,26 @@ void destroy(void* p) {
     delete static_cast<PartitionInfo<T, D>*>(p);
 }
 
+// Dimensions 1-3 are the reference's own instantiations (src/interface.cpp:128-141);
+// 4-8 follow its README recipe for more dimensions (more template instantiations).
+#define TK_DISPATCH_T(tree_dims, TT, CALL)                                         \
+    do {                                                                           \
+        using T = TT;                                                              \
+        switch (tree_dims) {                                                       \
+            case 1: { constexpr dim_t D = 1; CALL; break; }                        \
+            case 2: { constexpr dim_t D = 2; CALL; break; }                        \
+            case 3: { constexpr dim_t D = 3; CALL; break; }                        \
+            case 4: { constexpr dim_t D = 4; CALL; break; }                        \
+            case 5: { constexpr dim_t D = 5; CALL; break; }                        \
+            case 6: { constexpr dim_t D = 6; CALL; break; }                        \
+            case 7: { constexpr dim_t D = 7; CALL; break; }                        \
+            default: { constexpr dim_t D = 8; CALL; break; }                       \
+        }                                                                          \
+    } while (0)
 #define TK_DISPATCH(tree_dims, tree_dtype, CALL)                                   \
     do {                                                                           \
-        if ((tree_dtype) == 0) {                                                   \
-            if ((tree_dims) == 1) { using T = float; constexpr dim_t D = 1; CALL; } \
-            else if ((tree_dims) == 2) { using T = float; constexpr dim_t D = 2; CALL; } \
-            else { using T = float; constexpr dim_t D = 3; CALL; }                 \
-        } else {                                                                   \
-            if ((tree_dims) == 1) { using T = double; constexpr dim_t D = 1; CALL; } \
-            else if ((tree_dims) == 2) { using T = double; constexpr dim_t D = 2; CALL; } \
-            else { using T = double; constexpr dim_t D = 3; CALL; }                \
-        }                                                                          \
+        if ((tree_dtype) == 0) TK_DISPATCH_T(tree_dims, float, CALL);              \
+        else TK_DISPATCH_T(tree_dims, double, CALL);                               \
     } while (0)
 
 }  // namespace
@@ -75,7 +90,7 @@ extern "C" {
 const char* ref_last_error(void) { return g_err.c_str(); }
 
 void* ref_tree_create(const void* pts, int32_t n, int dims, int dtype, int levels) {
-    if (dims < 1 || dims > 3 || (dtype != 0 && dtype != 1)) {
+    if (dims < 1 || dims > 8 || (dtype != 0 && dtype != 1)) {
         g_err = "unsupported dims/dtype";
         return nullptr;
     }

@@ -7,7 +7,7 @@ indices, split planes, leaves) and its query output (squared distances and
 original indices).  Inputs are regenerated from their seed by
 ``golden_inputs()`` and guarded by a checksum, so the fixtures stay small.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [--force]
 
 The fixtures pin the oracle (tests/test_oracle.py) and serve as a second,
 reference-produced check of the GPU path (tests/test_kdtree_gpu.py).
@@ -32,6 +32,11 @@ CASES = [
     ("ties_f32_d3_grid", "f32", 3, 2000, 300, 8, None, "intgrid", True),
     ("ties_f64_d2_grid", "f64", 2, 1500, 200, 6, None, "intgrid", True),
     ("dup5pct_f32_d3", "f32", 3, 5000, 400, 16, None, "dup5", True),
+    # more dimensions, as the reference's README recipe compiles them
+    *[(f"wide_{dt}_d{d}_n{n}_q{nq}_k{k}", dt, d, n, nq, k, None, "normal1e3", True)
+      for (dt, d, n, nq, k) in (("f32", 4, 1000, 200, 10), ("f32", 5, 10000, 300, 20), ("f32", 8, 10000, 300, 16),
+                                ("f64", 6, 1000, 200, 10), ("f64", 8, 5000, 200, 33), ("f32", 7, 30, 20, 5))],
+    ("wide_ties_f32_d4_grid", "f32", 4, 2000, 300, 8, None, "intgrid", True),
     # BASELINE config 1: N(0,1)*1e3, 100,000 refs, 10,000 queries, k=5, levels 13
     ("config1_f32_d3_n100000_q10000_k5", "f32", 3, 100000, 10000, 5, None, "normal1e3", False),
 ]
@@ -74,7 +79,10 @@ def main() -> None:
     from oracle import oracle as O
 
     O.build(ref=True)
+    force = "--force" in sys.argv
     for (name, dtype, d, n, nq, k, levels, kind, full) in CASES:
+        if not force and os.path.exists(os.path.join(HERE, name + ".npz")):
+            continue  # fixtures are deterministic; regenerate all with --force
         ref, q = golden_inputs(name, dtype, d, n, nq, kind)
         T = O.RefTree(ref, levels)
         lay = T.layout()
