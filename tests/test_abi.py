@@ -63,7 +63,10 @@ def layout_of(h, n, d, levels, dtype):
 @pytest.mark.parametrize("name", [
     "grid_f32_d1_n1000_q200_k10", "grid_f32_d2_n10000_q300_k20", "grid_f32_d3_n10000_q300_k20",
     "grid_f64_d1_n10000_q300_k20", "grid_f64_d3_n1000_q200_k10", "grid_f32_d3_n30_q20_k5",
-    "grid_f64_d2_n5_q5_k1", "levels_f32_d3_n1000_L9", "levels_f32_d3_n1000_L1"])
+    "grid_f64_d2_n5_q5_k1", "levels_f32_d3_n1000_L9", "levels_f32_d3_n1000_L1",
+    # 4-8 dimensions (the reference's README recipe)
+    "wide_f32_d4_n1000_q200_k10", "wide_f32_d5_n10000_q300_k20", "wide_f32_d8_n10000_q300_k16",
+    "wide_f64_d6_n1000_q200_k10", "wide_f64_d8_n5000_q200_k33", "wide_f32_d7_n30_q20_k5"])
 def test_host_build_matches_reference_layout(name, golden):
     from torch_kdtree_gb300._lib import LIB, check
     case = golden[name]
@@ -116,8 +119,8 @@ def test_error_paths_without_gpu():
     bad[3, 1] = np.nan
     st, _ = host_tree(bad, 2)
     assert st == TK_EINVAL and "NaN" in LIB.tk_last_error().decode()
-    four_d = rng.standard_normal((10, 4)).astype(np.float32)
-    st, _ = host_tree(four_d, 2)
+    nine_d = rng.standard_normal((10, 9)).astype(np.float32)
+    st, _ = host_tree(nine_d, 2)  # KD trees go up to 8 dimensions
     assert st == TK_EINVAL
     # a host-only tree refuses queries instead of computing anything on the CPU
     st, h = host_tree(pts, 2)

@@ -67,7 +67,7 @@ def clouds(dtype, d, n, seed):
 
 
 @pytest.mark.parametrize("dtype", [np.float32, np.float64])
-@pytest.mark.parametrize("d", [1, 2, 3])
+@pytest.mark.parametrize("d", [1, 2, 3, 4, 5, 8])
 def test_device_build_equals_host_build(dtype, d):
     for n in (1, 2, 3, 17, 1000, 65537):
         lmax = max(1, int(np.floor(np.log2(n))) + 1)  # leaf parents need >= 1 point: n >= 2^(L-1)

@@ -213,3 +213,66 @@ def test_nan_query_row_is_isolated(oracle):
     bd, bi = oracle.brute(ref, q[ok], 4)
     np.testing.assert_array_equal(d[ok], bd)
     np.testing.assert_array_equal(i[ok], bi)
+
+
+WIDE_FIXTURES = ["wide_f32_d4_n1000_q200_k10", "wide_f32_d5_n10000_q300_k20", "wide_f32_d8_n10000_q300_k16",
+                 "wide_f64_d6_n1000_q200_k10", "wide_f64_d8_n5000_q200_k33", "wide_f32_d7_n30_q20_k5",
+                 "wide_ties_f32_d4_grid"]
+
+
+@pytest.mark.parametrize("name", WIDE_FIXTURES)
+def test_wide_golden_fixtures(name, golden, oracle):
+    """Trees of 4-8 dimensions (the reference's README recipe) against the
+    reference's own outputs and the oracle's exhaustive answer."""
+    case = golden[name]
+    ref, q = inputs_of(case)
+    k = int(case["k"])
+    d, i = gpu_query(ref, q, k, levels=int(case["levels"]))
+    bd, bi = oracle.brute(ref, q, k)
+    np.testing.assert_array_equal(d, bd)
+    np.testing.assert_array_equal(i, bi)
+    r = rows(case)
+    cmp = oracle.compare_knn(case["dists"], case["idx"], d[:r], i[:r])
+    assert cmp.ok, cmp
+
+
+@pytest.mark.parametrize("dims", [4, 5, 6, 7, 8])
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_wide_trees_every_shape(dims, dtype, oracle):
+    rng = np.random.default_rng(60 + dims)
+    ref = rng.standard_normal((6000, dims)).astype(dtype)
+    q = (rng.standard_normal((1500, dims)) * 1.2).astype(dtype)
+    for k in (1, 5, 16, 17, 100):
+        bd, bi = oracle.brute(ref, q, k)
+        for levels in (1, 5, 9):
+            for tpq, boxes in ((0, 1), (1, 1), (1, 0), (32, 1), (8, 0)):
+                d, i = gpu_query(ref, q, k, levels=levels, threads_per_query=tpq, prune_boxes=boxes)
+                np.testing.assert_array_equal(d, bd, err_msg=f"k={k} L={levels} tpq={tpq} boxes={boxes}")
+                np.testing.assert_array_equal(i, bi)
+
+
+def test_wide_tree_build_save_load_and_grad(tmp_path, oracle):
+    """GPU build, host build and a saved / re-loaded tree agree for a wide
+    cloud; gradients flow as for 3-D trees; batches refuse wide trees."""
+    rng = np.random.default_rng(66)
+    ref = rng.standard_normal((20000, 6)).astype(np.float32)
+    q = rng.standard_normal((3000, 6)).astype(np.float32)
+    rt, qt = torch.from_numpy(ref).to(cuda), torch.from_numpy(q).to(cuda)
+    th = tk().build_kd_tree(rt, build="host", levels=11)
+    td = tk().build_kd_tree(rt, build="device", levels=11)
+    assert torch.equal(th.shuffled_ind, td.shuffled_ind)
+    assert torch.equal(th.structured_points, td.structured_points)
+    td.save(tmp_path / "wide.npz")
+    tl = tk().load_kd_tree(tmp_path / "wide.npz")
+    bd, bi = oracle.brute(ref, q, 9)
+    for t in (th, td, tl):
+        d, i = t.query(qt, nr_nns_searches=9)
+        np.testing.assert_array_equal(d.cpu().numpy(), bd)
+        np.testing.assert_array_equal(i.cpu().numpy(), bi)
+    qg = qt.clone().requires_grad_(True)
+    d, i = td.query(qg, nr_nns_searches=3)
+    d.sum().backward()
+    assert torch.allclose(qg.grad, 2 * (qg[:, None] - rt[i.long()]).sum(1))
+    from torch_kdtree_gb300.batched import BatchedKDTrees
+    with pytest.raises(Exception):
+        BatchedKDTrees([rt], [4], [10])

@@ -268,6 +268,10 @@ int tk_batch_create(const tk_tree* const* trees, int n_trees, const int64_t* q_c
     b->n_clouds = n_trees;
     b->dtype = trees[0] ? trees[0]->dtype : TK_F32;
     b->dims = trees[0] ? trees[0]->dims : 0;
+    if (b->dims > 3) {
+        delete b;
+        return fail(TK_EUNSUPPORTED, "batched queries take trees of 1 to 3 dimensions (query wider trees one by one)");
+    }
     b->device = trees[0] ? trees[0]->device : 0;
     b->q_prefix.assign(n_trees + 1, 0);
     b->out_off.assign(n_trees, 0);

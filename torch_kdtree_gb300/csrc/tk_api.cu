@@ -7,6 +7,7 @@
 #include <vector>
 
 #include "kd_query.cuh"
+#include "kd_wide.cuh"
 #include "sort.cuh"
 #include "tk_internal.h"
 
@@ -124,6 +125,42 @@ int pow2_ceil(int v) {
     return p;
 }
 
+// Zero the work counter and, when binning is on, order the queries by the
+// tree cell at depth B they fall into (count, exclusive scan, scatter).
+// `count(B, counts, bin_of, pos_of)` launches the counting kernel.
+template <typename CountFn>
+int prepare_order(const tk_tree* t, int nq, const tk_query_opts& o, char* ws, cudaStream_t s, int** counter,
+                  const int32_t** order, CountFn count) {
+    const int L = t->levels;
+    const WsLayout w = ws_layout(L, nq);
+    *counter = reinterpret_cast<int*>(ws + w.counter);
+    *order = nullptr;
+    const bool bin = o.bin_queries == 1 || (o.bin_queries < 0 && nq >= 1024 && L >= 2);
+    cudaError_t e;
+    if (bin) {
+        const int B = bin_levels(L, nq);
+        const int nbins = 1 << B;
+        int* counts = reinterpret_cast<int*>(ws + w.counts);
+        int* bin_of = reinterpret_cast<int*>(ws + w.bin_of);
+        int* pos_of = reinterpret_cast<int*>(ws + w.pos_of);
+        int* ord = reinterpret_cast<int*>(ws + w.order);
+        e = cudaMemsetAsync(counts, 0, sizeof(int) * nbins, s);
+        if (e == cudaSuccess) e = cudaMemsetAsync(*counter, 0, sizeof(int), s);
+        if (e != cudaSuccess) return fail(TK_ECUDA, std::string("memset: ") + cudaGetErrorString(e));
+        count(B, counts, bin_of, pos_of);
+        e = exclusive_scan(counts, nbins, ws + w.scan, s);
+        if (e != cudaSuccess) return fail(TK_ECUDA, std::string("bin scan: ") + cudaGetErrorString(e));
+        k_bin_scatter<<<(nq + 255) / 256, 256, 0, s>>>(nq, bin_of, pos_of, counts, ord);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return fail(TK_ECUDA, std::string("binning launch: ") + cudaGetErrorString(e));
+        *order = ord;
+    } else {
+        e = cudaMemsetAsync(*counter, 0, sizeof(int), s);
+        if (e != cudaSuccess) return fail(TK_ECUDA, std::string("memset: ") + cudaGetErrorString(e));
+    }
+    return TK_OK;
+}
+
 template <typename T, int D>
 int run_query(const tk_tree* t, const T* q, int nq, int k, T* dists, int32_t* idx, const tk_query_opts& o,
               char* ws, cudaStream_t s) {
@@ -167,31 +204,12 @@ int run_query(const tk_tree* t, const T* q, int nq, int k, T* dists, int32_t* id
     const int need = (nq + groups_per_block - 1) / groups_per_block;
     const int grid = std::max(1, std::min(need, per_sm * sm_count(t->device)));
 
-    const WsLayout w = ws_layout(L, nq);
-    int* counter = reinterpret_cast<int*>(ws + w.counter);
-    const bool bin = o.bin_queries == 1 || (o.bin_queries < 0 && nq >= 1024 && L >= 2);
+    int* counter = nullptr;
     const int32_t* order = nullptr;
-    if (bin) {
-        const int B = bin_levels(L, nq);
-        const int nbins = 1 << B;
-        int* counts = reinterpret_cast<int*>(ws + w.counts);
-        int* bin_of = reinterpret_cast<int*>(ws + w.bin_of);
-        int* pos_of = reinterpret_cast<int*>(ws + w.pos_of);
-        int* ord = reinterpret_cast<int*>(ws + w.order);
-        e = cudaMemsetAsync(counts, 0, sizeof(int) * nbins, s);
-        if (e == cudaSuccess) e = cudaMemsetAsync(counter, 0, sizeof(int), s);
-        if (e != cudaSuccess) return fail(TK_ECUDA, std::string("memset: ") + cudaGetErrorString(e));
+    int rc0 = prepare_order(t, nq, o, ws, s, &counter, &order, [&](int B, int* counts, int* bin_of, int* pos_of) {
         bin_count_launch<T, D>(q, nq, static_cast<const T*>(t->d_medians), B, counts, bin_of, pos_of, s);
-        e = exclusive_scan(counts, nbins, ws + w.scan, s);
-        if (e != cudaSuccess) return fail(TK_ECUDA, std::string("bin scan: ") + cudaGetErrorString(e));
-        k_bin_scatter<<<(nq + 255) / 256, 256, 0, s>>>(nq, bin_of, pos_of, counts, ord);
-        e = cudaGetLastError();
-        if (e != cudaSuccess) return fail(TK_ECUDA, std::string("binning launch: ") + cudaGetErrorString(e));
-        order = ord;
-    } else {
-        e = cudaMemsetAsync(counter, 0, sizeof(int), s);
-        if (e != cudaSuccess) return fail(TK_ECUDA, std::string("memset: ") + cudaGetErrorString(e));
-    }
+    });
+    if (rc0 != TK_OK) return rc0;
 
     KdArgs<T> a;
     a.pts = static_cast<const PointRec<T>*>(t->d_pts);
@@ -214,6 +232,68 @@ int run_query(const tk_tree* t, const T* q, int nq, int k, T* dists, int32_t* id
     return rc;
 }
 
+// KD query of a tree of 4-8 dimensions (kd_wide.cuh): one lane per query
+// for k <= 16 when the automatic / requested shape is one lane, else a
+// 32-lane group per query; binning and options as run_query (warp packets do
+// not apply: traversal 2 runs as 1).
+template <typename T>
+int run_query_wide(const tk_tree* t, const T* q, int nq, int k, T* dists, int32_t* idx, const tk_query_opts& o,
+                   char* ws, cudaStream_t s) {
+    if (o.traversal < 0 || o.traversal > 2) return fail(TK_EINVAL, "traversal must be 0, 1 or 2");
+    int G = o.threads_per_query > 0 ? o.threads_per_query : auto_lanes(t, nq, k);
+    if (G != 1 && G != 2 && G != 4 && G != 8 && G != 16 && G != 32)
+        return fail(TK_EINVAL, "threads_per_query must be 1, 2, 4, 8, 16 or 32");
+    if (G != 1 || k > 16) G = 32;  // kernels of wide trees: 1 or 32 lanes per query
+    const int R = G == 1 ? pow2_ceil(k) : pow2_ceil((k + 31) / 32);
+    const int W = record_width(t->dims);
+    const int L = t->levels;
+    int S = o.smem_levels >= 0 ? o.smem_levels : 10;
+    S = std::max(0, std::min({S, L, sizeof(T) == 4 ? 15 : 14}));
+    const int block = kKdBlock;
+    const size_t smem = kd_smem_bytes<T>(S);
+    const void* kfn = kd_wide_kernel<T>(W, G, R);
+    if (!kfn) return fail(TK_EUNSUPPORTED, "KD query kernel shape not compiled");
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+        if (e != cudaSuccess) return fail(TK_ECUDA, std::string("smem attribute: ") + cudaGetErrorString(e));
+    }
+    int per_sm = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, block, smem);
+    if (e != cudaSuccess || per_sm <= 0) per_sm = 1;
+    if (o.blocks_per_sm > 0) per_sm = std::min(per_sm, int(o.blocks_per_sm));
+    const int groups_per_block = block / G;
+    const int need = (nq + groups_per_block - 1) / groups_per_block;
+    const int grid = std::max(1, std::min(need, per_sm * sm_count(t->device)));
+
+    int* counter = nullptr;
+    const int32_t* order = nullptr;
+    const int rc0 = prepare_order(t, nq, o, ws, s, &counter, &order, [&](int B, int* counts, int* bin_of, int* pos_of) {
+        bin_count_wide_launch<T>(q, nq, t->dims, static_cast<const T*>(t->d_medians), B, counts, bin_of, pos_of, s);
+    });
+    if (rc0 != TK_OK) return rc0;
+
+    KdWideArgs<T> a;
+    a.pts = static_cast<const T*>(t->d_pts);
+    a.perm = t->d_perm;
+    a.medians = static_cast<const T*>(t->d_medians);
+    a.leaf_off = t->d_leaf_off;
+    a.boxes = o.prune_boxes == 0 ? nullptr : static_cast<const T*>(t->d_boxes);
+    a.levels = L;
+    a.smem_levels = S;
+    a.dims = t->dims;
+    a.q = q;
+    a.nq = nq;
+    a.k = k;
+    a.order = order;
+    a.out_d = dists;
+    a.out_i = idx;
+    a.work = counter;
+    if (o.kernel_start_event) cudaEventRecord(static_cast<cudaEvent_t>(o.kernel_start_event), s);
+    const int rc = kd_wide_launch<T>(a, W, G, R, grid, block, smem, s);
+    if (rc == TK_OK && o.kernel_stop_event) cudaEventRecord(static_cast<cudaEvent_t>(o.kernel_stop_event), s);
+    return rc;
+}
+
 // The 4th slot of a point record holds an index as raw bits: the original
 // index of a point, or the begin / end offset of a leaf in its box records.
 template <typename T>
@@ -226,8 +306,46 @@ void set_rec_index(PointRec<T>& r, uint32_t v) {
     }
 }
 
+// Device image of a tree of 4-8 dimensions: zero-padded coordinate rows of
+// record_width(dims), the original indices, and node boxes as lo / hi rows.
+template <typename T>
+int upload_wide(tk_tree* t, const HostTree<T>& h) {
+    const int64_t n = h.n;
+    const int W = record_width(h.dims);
+    std::vector<T> rows(static_cast<size_t>(n) * W, T(0));
+    for (int64_t i = 0; i < n; ++i)
+        for (int d = 0; d < h.dims; ++d) rows[size_t(i) * W + d] = h.structured[i * h.dims + d];
+    const size_t nnodes = h.box_lo.size() / W;
+    std::vector<T> boxes(2 * nnodes * W);
+    for (size_t i = 0; i < nnodes; ++i)
+        for (int c = 0; c < W; ++c) {
+            boxes[(2 * i) * W + c] = h.box_lo[i * W + c];
+            boxes[(2 * i + 1) * W + c] = h.box_hi[i * W + c];
+        }
+    const size_t b_pts = sizeof(T) * rows.size();
+    const size_t b_perm = sizeof(int32_t) * size_t(n);
+    const size_t b_med = sizeof(T) * h.medians.size();
+    const size_t b_off = sizeof(int32_t) * h.leaf_off.size();
+    const size_t b_box = sizeof(T) * boxes.size();
+    cudaError_t e = cudaMalloc(&t->d_pts, b_pts);
+    if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&t->d_perm), b_perm);
+    if (e == cudaSuccess) e = cudaMalloc(&t->d_medians, std::max<size_t>(b_med, sizeof(T)));
+    if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&t->d_leaf_off), b_off);
+    if (e == cudaSuccess) e = cudaMalloc(&t->d_boxes, b_box);
+    if (e != cudaSuccess) return fail(TK_ENOMEM, std::string("device allocation: ") + cudaGetErrorString(e));
+    e = cudaMemcpy(t->d_pts, rows.data(), b_pts, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(t->d_perm, h.perm.data(), b_perm, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && b_med) e = cudaMemcpy(t->d_medians, h.medians.data(), b_med, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(t->d_leaf_off, h.leaf_off.data(), b_off, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(t->d_boxes, boxes.data(), b_box, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return fail(TK_ECUDA, std::string("tree upload: ") + cudaGetErrorString(e));
+    t->device_bytes = int64_t(b_pts + b_perm + b_med + b_off + b_box);
+    return TK_OK;
+}
+
 template <typename T>
 int upload_tree(tk_tree* t, const HostTree<T>& h) {
+    if (h.dims > 3) return upload_wide(t, h);
     const int64_t n = h.n;
     std::vector<PointRec<T>> recs(static_cast<size_t>(n));
     for (int64_t i = 0; i < n; ++i) {
@@ -269,6 +387,8 @@ int upload_tree(tk_tree* t, const HostTree<T>& h) {
 
 void free_tree_device(tk_tree* t) {
     if (t->d_pts) cudaFree(t->d_pts);
+    if (t->d_perm) cudaFree(t->d_perm);
+    t->d_perm = nullptr;
     if (t->d_medians) cudaFree(t->d_medians);
     if (t->d_leaf_off) cudaFree(t->d_leaf_off);
     if (t->d_boxes) cudaFree(t->d_boxes);
@@ -281,6 +401,21 @@ void free_tree_device(tk_tree* t) {
 template <typename T>
 int device_layout(const tk_tree* t, T* points, int32_t* perm) {
     DeviceGuard g(t->device);
+    if (t->dims > 3) {  // coordinate rows + separate indices
+        const int W = record_width(t->dims);
+        cudaError_t e = cudaSuccess;
+        if (points) {
+            std::vector<T> rows(static_cast<size_t>(t->n) * W);
+            e = cudaMemcpy(rows.data(), t->d_pts, sizeof(T) * rows.size(), cudaMemcpyDeviceToHost);
+            if (e == cudaSuccess)
+                for (int64_t i = 0; i < t->n; ++i)
+                    for (int d = 0; d < t->dims; ++d) points[i * t->dims + d] = rows[size_t(i) * W + d];
+        }
+        if (e == cudaSuccess && perm)
+            e = cudaMemcpy(perm, t->d_perm, sizeof(int32_t) * size_t(t->n), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return fail(TK_ECUDA, std::string("layout copy: ") + cudaGetErrorString(e));
+        return TK_OK;
+    }
     std::vector<PointRec<T>> recs(static_cast<size_t>(t->n));
     const cudaError_t e = cudaMemcpy(recs.data(), t->d_pts, sizeof(PointRec<T>) * recs.size(), cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return fail(TK_ECUDA, std::string("layout copy: ") + cudaGetErrorString(e));
@@ -415,8 +550,9 @@ int tk_tree_create_device(const void* dev_points, int64_t n, int dims, int dtype
     *out = nullptr;
     if (dtype != TK_F32 && dtype != TK_F64) return fail(TK_EINVAL, "dtype must be TK_F32 or TK_F64");
     if (!dev_points) return fail(TK_EINVAL, "points pointer is null");
-    if (dims < 1 || dims > 3)
-        return fail(TK_EINVAL, "KD-tree supports dims 1, 2 or 3 (got " + std::to_string(dims) + ")");
+    if (dims < 1 || dims > kMaxDims)
+        return fail(TK_EINVAL, "KD-tree supports dims 1 to " + std::to_string(kMaxDims) + " (got " +
+                                   std::to_string(dims) + ")");
     if (n < 1) return fail(TK_EINVAL, "the reference point cloud is empty");
     if (n >= (int64_t(1) << 31)) return fail(TK_EINVAL, "only 32 bit signed indexing implemented (n < 2^31)");
     if (levels < 1 || levels > kMaxLevels)
@@ -561,7 +697,8 @@ int tk_tree_query(const tk_tree* t, const void* q, int64_t nq, int k, void* dist
         switch (t->dims) {
             case 1: return run_query<float, 1>(t, qq, n32, k, dd, idx, o, ws, s);
             case 2: return run_query<float, 2>(t, qq, n32, k, dd, idx, o, ws, s);
-            default: return run_query<float, 3>(t, qq, n32, k, dd, idx, o, ws, s);
+            case 3: return run_query<float, 3>(t, qq, n32, k, dd, idx, o, ws, s);
+            default: return run_query_wide<float>(t, qq, n32, k, dd, idx, o, ws, s);
         }
     } else {
         auto* qq = static_cast<const double*>(q);
@@ -569,7 +706,8 @@ int tk_tree_query(const tk_tree* t, const void* q, int64_t nq, int k, void* dist
         switch (t->dims) {
             case 1: return run_query<double, 1>(t, qq, n32, k, dd, idx, o, ws, s);
             case 2: return run_query<double, 2>(t, qq, n32, k, dd, idx, o, ws, s);
-            default: return run_query<double, 3>(t, qq, n32, k, dd, idx, o, ws, s);
+            case 3: return run_query<double, 3>(t, qq, n32, k, dd, idx, o, ws, s);
+            default: return run_query_wide<double>(t, qq, n32, k, dd, idx, o, ws, s);
         }
     }
 }
@@ -645,7 +783,8 @@ extern "C" int tk_tree_query_noalloc(const tk_tree* t, const void* q, int64_t nq
         switch (t->dims) {
             case 1: return run_query<float, 1>(t, qq, n32, k, dd, idx, o, ws, s);
             case 2: return run_query<float, 2>(t, qq, n32, k, dd, idx, o, ws, s);
-            default: return run_query<float, 3>(t, qq, n32, k, dd, idx, o, ws, s);
+            case 3: return run_query<float, 3>(t, qq, n32, k, dd, idx, o, ws, s);
+            default: return run_query_wide<float>(t, qq, n32, k, dd, idx, o, ws, s);
         }
     }
     auto* qq = static_cast<const double*>(q);
@@ -653,6 +792,7 @@ extern "C" int tk_tree_query_noalloc(const tk_tree* t, const void* q, int64_t nq
     switch (t->dims) {
         case 1: return run_query<double, 1>(t, qq, n32, k, dd, idx, o, ws, s);
         case 2: return run_query<double, 2>(t, qq, n32, k, dd, idx, o, ws, s);
-        default: return run_query<double, 3>(t, qq, n32, k, dd, idx, o, ws, s);
+        case 3: return run_query<double, 3>(t, qq, n32, k, dd, idx, o, ws, s);
+        default: return run_query_wide<double>(t, qq, n32, k, dd, idx, o, ws, s);
     }
 }

@@ -13,6 +13,12 @@ namespace tk {
 constexpr int kMaxLevels = 24;   // 2^24 leaves; the stack of a traversal holds <= kMaxLevels entries
 constexpr int kMaxK = 128;       // reference GPU cap (src/kdtree_g.cu:283,421)
 constexpr int kMaxBinLevels = 16;
+constexpr int kMaxDims = 8;      // KD-tree dimensions (brute force: up to 128)
+
+// Coordinates per device point record of a tree of `dims` dimensions: up to
+// 3 share one 16-byte record with the original index; 4 or 5-8 dimensions use
+// 4 or 8 zero-padded coordinates with the indices in a separate array.
+inline int record_width(int dims) { return dims <= 3 ? 3 : (dims <= 4 ? 4 : 8); }
 
 // Sets the thread-local error text and returns the status.
 int fail(int status, const std::string& msg);
@@ -30,9 +36,10 @@ struct HostTree {
     std::vector<T> medians;           // [2^L - 1] heap order; axis = depth % dims
     std::vector<int32_t> leaf_off;    // [2^L + 1] prefix offsets of the leaves
     // Tight bounding boxes of every node's points, heap order over all
-    // 2^(L+1) - 1 nodes (leaves last), 3 coordinates each (unused ones 0);
-    // empty nodes have lo = +inf, hi = -inf.
+    // 2^(L+1) - 1 nodes (leaves last), box_stride() coordinates each (unused
+    // ones 0); empty nodes have lo = +inf, hi = -inf.
     std::vector<T> box_lo, box_hi;
+    int box_stride() const { return record_width(dims); }
 };
 
 // Builds the tree (tree_build.cpp).  Returns TK_OK or sets the error.
@@ -76,6 +83,7 @@ struct tk_tree {
     void* d_pts = nullptr;       // point records: coordinates + original index (see tk_device.cuh)
     void* d_medians = nullptr;   // T[2^L - 1]
     int32_t* d_leaf_off = nullptr;  // int32[2^L + 1]
-    void* d_boxes = nullptr;     // per node {lo.xyz, 0}, {hi.xyz, 0} (see tk_device.cuh)
+    void* d_boxes = nullptr;     // per node {lo.xyz, 0}, {hi.xyz, 0} (see tk_device.cuh); lo / hi rows when wide
+    int32_t* d_perm = nullptr;   // trees of 4-8 dims: original index of each point (records hold coordinates only)
     int64_t device_bytes = 0;
 };

@@ -27,23 +27,25 @@
 namespace tk {
 namespace {
 
-template <typename T>
+// NC coordinates per record: 3 for clouds of up to 3 dimensions, 8 above.
+template <typename T, int NC>
 struct Rec {
-    T c[3];
+    T c[NC];
     int32_t orig;
 };
 
-template <typename T>
+template <typename T, int NC>
 struct Builder {
+    using R = Rec<T, NC>;
     int dims;
     int levels;
     int32_t nparts;
-    Rec<T>* recs;
+    R* recs;
     T* medians;
     int32_t* leaf_off;
     std::atomic<bool> failed{false};  // set by any worker that meets an empty split node
 
-    static bool less(const Rec<T>& a, const Rec<T>& b, int ax) {
+    static bool less(const R& a, const R& b, int ax) {
         if (a.c[ax] < b.c[ax]) return true;
         if (b.c[ax] < a.c[ax]) return false;
         return a.orig < b.orig;
@@ -62,9 +64,9 @@ struct Builder {
             return;
         }
         const int ax = depth % dims;
-        Rec<T>* r = recs + lo;
+        R* r = recs + lo;
         const int32_t h = n / 2;
-        auto cmp = [ax](const Rec<T>& a, const Rec<T>& b) { return less(a, b, ax); };
+        auto cmp = [ax](const R& a, const R& b) { return less(a, b, ax); };
         if (depth == levels - 1) {
             std::sort(r, r + n, cmp);
             medians[id] = median_of(h > 0 ? r[h - 1].c[ax] : r[h].c[ax], r[h].c[ax], n);
@@ -89,18 +91,20 @@ struct Builder {
 };
 
 // Tight bounding box of every node's points: leaves from their points,
-// inner nodes from their children; heap order over all 2^(L+1) - 1 nodes.
+// inner nodes from their children; heap order over all 2^(L+1) - 1 nodes,
+// box_stride() coordinates per node (unused ones 0; empty nodes +inf / -inf).
 template <typename T>
 void compute_boxes(HostTree<T>& out) {
+    const int bs = out.box_stride();
     const int64_t nleaves = int64_t(1) << out.levels;
     const int64_t nnodes = 2 * nleaves - 1;
     const T inf = std::numeric_limits<T>::infinity();
-    out.box_lo.assign(static_cast<size_t>(nnodes) * 3, inf);
-    out.box_hi.assign(static_cast<size_t>(nnodes) * 3, -inf);
+    out.box_lo.assign(static_cast<size_t>(nnodes) * bs, inf);
+    out.box_hi.assign(static_cast<size_t>(nnodes) * bs, -inf);
     for (int64_t l = 0; l < nleaves; ++l) {
         const int64_t node = nleaves - 1 + l;
-        T* lo = &out.box_lo[node * 3];
-        T* hi = &out.box_hi[node * 3];
+        T* lo = &out.box_lo[node * bs];
+        T* hi = &out.box_hi[node * bs];
         for (int32_t i = out.leaf_off[l]; i < out.leaf_off[l + 1]; ++i)
             for (int c = 0; c < out.dims; ++c) {
                 const T v = out.structured[size_t(i) * out.dims + c];
@@ -108,13 +112,42 @@ void compute_boxes(HostTree<T>& out) {
                 hi[c] = std::max(hi[c], v);
             }
         if (out.leaf_off[l + 1] > out.leaf_off[l])
-            for (int c = out.dims; c < 3; ++c) lo[c] = hi[c] = T(0);  // unused coordinates are 0
+            for (int c = out.dims; c < bs; ++c) lo[c] = hi[c] = T(0);  // unused coordinates are 0
     }
     for (int64_t node = nleaves - 2; node >= 0; --node)
-        for (int c = 0; c < 3; ++c) {
-            out.box_lo[node * 3 + c] = std::min(out.box_lo[(2 * node + 1) * 3 + c], out.box_lo[(2 * node + 2) * 3 + c]);
-            out.box_hi[node * 3 + c] = std::max(out.box_hi[(2 * node + 1) * 3 + c], out.box_hi[(2 * node + 2) * 3 + c]);
+        for (int c = 0; c < bs; ++c) {
+            out.box_lo[node * bs + c] = std::min(out.box_lo[(2 * node + 1) * bs + c], out.box_lo[(2 * node + 2) * bs + c]);
+            out.box_hi[node * bs + c] = std::max(out.box_hi[(2 * node + 1) * bs + c], out.box_hi[(2 * node + 2) * bs + c]);
         }
+}
+
+template <typename T, int NC>
+bool run_builder(const T* pts, int64_t n, int dims, int levels, int n_threads, HostTree<T>& out) {
+    const int32_t nparts = int32_t((1u << levels) - 1u);
+    std::vector<Rec<T, NC>> recs(static_cast<size_t>(n));
+    for (int64_t i = 0; i < n; ++i) {
+        for (int c = 0; c < NC; ++c) recs[i].c[c] = c < dims ? pts[i * dims + c] : T(0);
+        recs[i].orig = int32_t(i);
+    }
+    if (n_threads <= 0) n_threads = int(std::max(1u, std::thread::hardware_concurrency()));
+    int spawn_depth = 0;
+    while ((1 << spawn_depth) < n_threads && spawn_depth < 8) ++spawn_depth;
+    Builder<T, NC> b;
+    b.dims = dims;
+    b.levels = levels;
+    b.nparts = nparts;
+    b.recs = recs.data();
+    b.medians = out.medians.data();
+    b.leaf_off = out.leaf_off.data();
+    b.node(0, int32_t(n), 0, 0, spawn_depth);
+    if (b.failed.load()) return false;
+    out.structured.resize(static_cast<size_t>(n) * dims);
+    out.perm.resize(static_cast<size_t>(n));
+    for (int64_t i = 0; i < n; ++i) {
+        for (int c = 0; c < dims; ++c) out.structured[i * dims + c] = recs[i].c[c];
+        out.perm[i] = recs[i].orig;
+    }
+    return true;
 }
 
 }  // namespace
@@ -122,8 +155,9 @@ void compute_boxes(HostTree<T>& out) {
 template <typename T>
 int build_host_tree(const T* pts, int64_t n, int dims, int levels, int n_threads, HostTree<T>& out) {
     if (pts == nullptr) return fail(TK_EINVAL, "points pointer is null");
-    if (dims < 1 || dims > 3)
-        return fail(TK_EINVAL, "KD-tree supports dims 1, 2 or 3 (got " + std::to_string(dims) + ")");
+    if (dims < 1 || dims > kMaxDims)
+        return fail(TK_EINVAL, "KD-tree supports dims 1 to " + std::to_string(kMaxDims) + " (got " +
+                                   std::to_string(dims) + ")");
     if (n < 1) return fail(TK_EINVAL, "the reference point cloud is empty");
     if (n >= (int64_t(1) << 31)) return fail(TK_EINVAL, "only 32 bit signed indexing implemented (n < 2^31)");
     if (levels < 1 || levels > kMaxLevels)
@@ -132,41 +166,19 @@ int build_host_tree(const T* pts, int64_t n, int dims, int levels, int n_threads
         if (std::isnan(pts[i])) return fail(TK_EINVAL, "reference points contain NaN");
 
     const int32_t nparts = int32_t((1u << levels) - 1u);
-    std::vector<Rec<T>> recs(static_cast<size_t>(n));
-    for (int64_t i = 0; i < n; ++i) {
-        for (int c = 0; c < 3; ++c) recs[i].c[c] = c < dims ? pts[i * dims + c] : T(0);
-        recs[i].orig = int32_t(i);
-    }
     out.n = n;
     out.dims = dims;
     out.levels = levels;
     out.medians.assign(static_cast<size_t>(nparts), T(0));
     out.leaf_off.assign(static_cast<size_t>(nparts) + 2, 0);
-
-    if (n_threads <= 0) n_threads = int(std::max(1u, std::thread::hardware_concurrency()));
-    int spawn_depth = 0;
-    while ((1 << spawn_depth) < n_threads && spawn_depth < 8) ++spawn_depth;
-
-    Builder<T> b;
-    b.dims = dims;
-    b.levels = levels;
-    b.nparts = nparts;
-    b.recs = recs.data();
-    b.medians = out.medians.data();
-    b.leaf_off = out.leaf_off.data();
-    b.node(0, int32_t(n), 0, 0, spawn_depth);
-    if (b.failed.load())
+    const bool ok = dims <= 3 ? run_builder<T, 3>(pts, n, dims, levels, n_threads, out)
+                              : run_builder<T, 8>(pts, n, dims, levels, n_threads, out);
+    if (!ok)
         return fail(TK_EINVAL,
                     "Ran out of points while building KD-Tree. Either you required too many levels, "
                     "or you used a lot of coplanar points");
     out.leaf_off.resize(static_cast<size_t>(nparts) + 2);
     out.leaf_off[nparts + 1] = int32_t(n);  // 2^L leaves -> 2^L + 1 offsets
-    out.structured.resize(static_cast<size_t>(n) * dims);
-    out.perm.resize(static_cast<size_t>(n));
-    for (int64_t i = 0; i < n; ++i) {
-        for (int c = 0; c < dims; ++c) out.structured[i * dims + c] = recs[i].c[c];
-        out.perm[i] = recs[i].orig;
-    }
     compute_boxes(out);
     return TK_OK;
 }
@@ -175,8 +187,9 @@ template <typename T>
 int tree_from_layout(const T* structured, const int32_t* perm, const T* medians, const int32_t* leaf_off, int64_t n,
                      int dims, int levels, HostTree<T>& out) {
     if (!structured || !perm || !medians || !leaf_off) return fail(TK_EINVAL, "layout pointer is null");
-    if (dims < 1 || dims > 3)
-        return fail(TK_EINVAL, "KD-tree supports dims 1, 2 or 3 (got " + std::to_string(dims) + ")");
+    if (dims < 1 || dims > kMaxDims)
+        return fail(TK_EINVAL, "KD-tree supports dims 1 to " + std::to_string(kMaxDims) + " (got " +
+                                   std::to_string(dims) + ")");
     if (n < 1) return fail(TK_EINVAL, "the reference point cloud is empty");
     if (n >= (int64_t(1) << 31)) return fail(TK_EINVAL, "only 32 bit signed indexing implemented (n < 2^31)");
     if (levels < 1 || levels > kMaxLevels)
@@ -213,8 +226,9 @@ int tree_from_layout(const T* structured, const int32_t* perm, const T* medians,
         const int depth = 63 - __builtin_clzll(uint64_t(node + 1));
         const int ax = depth % dims;
         const T m = out.medians[size_t(node)];
-        const T left_hi = out.box_hi[size_t(2 * node + 1) * 3 + ax];
-        const T right_lo = out.box_lo[size_t(2 * node + 2) * 3 + ax];
+        const int bs = out.box_stride();
+        const T left_hi = out.box_hi[size_t(2 * node + 1) * bs + ax];
+        const T right_lo = out.box_lo[size_t(2 * node + 2) * bs + ax];
         if (left_hi > m || right_lo < m)
             return fail(TK_EINVAL, "layout is inconsistent: points on the wrong side of split " + std::to_string(node));
     }

@@ -234,6 +234,74 @@ __global__ void k_inner_boxes(int nodes, PointRec<T>* __restrict__ boxes) {
     boxes[2 * id + 1] = hi;
 }
 
+// Trees of 4-8 dimensions: coordinate rows of W (zero padded) and the
+// original indices, in leaf order.
+template <typename T>
+__global__ void k_make_rows(const T* __restrict__ pts, int dims, int W, const uint32_t* __restrict__ order,
+                            int64_t n, T* __restrict__ rows, int32_t* __restrict__ perm) {
+    const int64_t p = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    const uint32_t id = order[p];
+    for (int d = 0; d < W; ++d) rows[p * W + d] = d < dims ? pts[int64_t(id) * dims + d] : T(0);
+    perm[p] = int32_t(id);
+}
+
+// Leaf boxes of such a tree (one warp per leaf): lo row at node 2i, hi at 2i+1.
+template <typename T>
+__global__ void k_leaf_boxes_wide(const T* __restrict__ rows, int W, const int32_t* __restrict__ leaf_off,
+                                  int64_t nleaves, T* __restrict__ boxes) {
+    const int64_t leaf = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (leaf >= nleaves) return;
+    const T inf = std::numeric_limits<T>::infinity();
+    T lo[kMaxDims], hi[kMaxDims];
+#pragma unroll
+    for (int d = 0; d < kMaxDims; ++d) {
+        lo[d] = inf;
+        hi[d] = -inf;
+    }
+    for (int32_t i = leaf_off[leaf] + lane; i < leaf_off[leaf + 1]; i += 32) {
+#pragma unroll
+        for (int d = 0; d < kMaxDims; ++d) {
+            if (d < W) {
+                const T c = rows[int64_t(i) * W + d];
+                lo[d] = c < lo[d] ? c : lo[d];
+                hi[d] = hi[d] < c ? c : hi[d];
+            }
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+        for (int d = 0; d < kMaxDims; ++d) {
+            const T l = __shfl_xor_sync(0xFFFFFFFFu, lo[d], o);
+            const T h = __shfl_xor_sync(0xFFFFFFFFu, hi[d], o);
+            lo[d] = l < lo[d] ? l : lo[d];
+            hi[d] = hi[d] < h ? h : hi[d];
+        }
+    }
+    if (lane == 0) {
+        const int64_t node = nleaves - 1 + leaf;
+        for (int d = 0; d < W; ++d) {
+            boxes[(2 * node) * W + d] = lo[d];
+            boxes[(2 * node + 1) * W + d] = hi[d];
+        }
+    }
+}
+
+template <typename T>
+__global__ void k_inner_boxes_wide(int nodes, int W, T* __restrict__ boxes) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= nodes) return;
+    const int64_t id = int64_t(nodes) - 1 + j, a = 2 * id + 1, b = 2 * id + 2;
+    for (int d = 0; d < W; ++d) {
+        const T al = boxes[(2 * a) * W + d], ah = boxes[(2 * a + 1) * W + d];
+        const T bl = boxes[(2 * b) * W + d], bh = boxes[(2 * b + 1) * W + d];
+        boxes[(2 * id) * W + d] = bl < al ? bl : al;
+        boxes[(2 * id + 1) * W + d] = ah < bh ? bh : ah;
+    }
+}
+
 // Device scratch of one build, freed on every exit path.
 struct Scratch {
     std::vector<void*> ptrs;
@@ -267,7 +335,7 @@ int build_device_tree(const T* pts, int64_t n, int dims, int levels, void* strea
     const int64_t nnodes = 2 * nleaves - 1;
 
     Scratch sc;
-    uint32_t* P[3] = {nullptr, nullptr, nullptr};
+    uint32_t* P[kMaxDims] = {};
     for (int a = 0; a < dims; ++a) P[a] = sc.get<uint32_t>(n);
     uint32_t* spare = sc.get<uint32_t>(n);
     uint32_t* key_lo = sc.get<uint32_t>(n);
@@ -285,16 +353,20 @@ int build_device_tree(const T* pts, int64_t n, int dims, int levels, void* strea
     void* scan_ws = sc.get<unsigned char>(scan_workspace_bytes(n));
     if (sc.err != cudaSuccess) return fail(TK_ENOMEM, std::string("device build scratch: ") + cudaGetErrorString(sc.err));
 
-    // the tree's device image
-    const size_t b_pts = sizeof(PointRec<T>) * size_t(n);
+    // the tree's device image (wide trees: coordinate rows, indices, box rows)
+    const bool wide = dims > 3;
+    const int W = record_width(dims);
+    const size_t b_pts = wide ? sizeof(T) * W * size_t(n) : sizeof(PointRec<T>) * size_t(n);
+    const size_t b_perm = wide ? sizeof(int32_t) * size_t(n) : 0;
     const size_t b_med = sizeof(T) * size_t(nparts);
     const size_t b_off = sizeof(int32_t) * size_t(nleaves + 1);
-    const size_t b_box = sizeof(PointRec<T>) * 2 * size_t(nnodes);
+    const size_t b_box = wide ? sizeof(T) * W * 2 * size_t(nnodes) : sizeof(PointRec<T>) * 2 * size_t(nnodes);
     TK_TRY(cudaMalloc(&t->d_pts, b_pts));
+    if (wide) TK_TRY(cudaMalloc(reinterpret_cast<void**>(&t->d_perm), b_perm));
     TK_TRY(cudaMalloc(&t->d_medians, std::max<size_t>(b_med, 16)));
     TK_TRY(cudaMalloc(reinterpret_cast<void**>(&t->d_leaf_off), b_off));
     TK_TRY(cudaMalloc(&t->d_boxes, b_box));
-    t->device_bytes = int64_t(b_pts + b_med + b_off + b_box);
+    t->device_bytes = int64_t(b_pts + b_perm + b_med + b_off + b_box);
     T* medians = static_cast<T*>(t->d_medians);
     PointRec<T>* recs = static_cast<PointRec<T>*>(t->d_pts);
     PointRec<T>* boxes = static_cast<PointRec<T>*>(t->d_boxes);
@@ -348,13 +420,26 @@ int build_device_tree(const T* pts, int64_t n, int dims, int levels, void* strea
     TK_TRY(cudaMemcpyAsync(t->d_leaf_off + nleaves, &n32, sizeof(int32_t), cudaMemcpyHostToDevice, s));
 
     // 4. records in leaf order, node boxes bottom-up
-    k_make_records<T><<<blocks_for(n), kThreads, 0, s>>>(pts, dims, P[(L - 1) % dims], n, recs);
-    k_leaf_boxes<T><<<unsigned((nleaves * 32 + kThreads - 1) / kThreads), kThreads, 0, s>>>(recs, t->d_leaf_off,
-                                                                                            nleaves, boxes);
-    TK_TRY(cudaGetLastError());
-    for (int lev = L - 1; lev >= 0; --lev) {
-        k_inner_boxes<T><<<blocks_for(int64_t(1) << lev), kThreads, 0, s>>>(1 << lev, boxes);
+    if (wide) {
+        T* rows = static_cast<T*>(t->d_pts);
+        T* wboxes = static_cast<T*>(t->d_boxes);
+        k_make_rows<T><<<blocks_for(n), kThreads, 0, s>>>(pts, dims, W, P[(L - 1) % dims], n, rows, t->d_perm);
+        k_leaf_boxes_wide<T><<<unsigned((nleaves * 32 + kThreads - 1) / kThreads), kThreads, 0, s>>>(
+            rows, W, t->d_leaf_off, nleaves, wboxes);
         TK_TRY(cudaGetLastError());
+        for (int lev = L - 1; lev >= 0; --lev) {
+            k_inner_boxes_wide<T><<<blocks_for(int64_t(1) << lev), kThreads, 0, s>>>(1 << lev, W, wboxes);
+            TK_TRY(cudaGetLastError());
+        }
+    } else {
+        k_make_records<T><<<blocks_for(n), kThreads, 0, s>>>(pts, dims, P[(L - 1) % dims], n, recs);
+        k_leaf_boxes<T><<<unsigned((nleaves * 32 + kThreads - 1) / kThreads), kThreads, 0, s>>>(recs, t->d_leaf_off,
+                                                                                                nleaves, boxes);
+        TK_TRY(cudaGetLastError());
+        for (int lev = L - 1; lev >= 0; --lev) {
+            k_inner_boxes<T><<<blocks_for(int64_t(1) << lev), kThreads, 0, s>>>(1 << lev, boxes);
+            TK_TRY(cudaGetLastError());
+        }
     }
     int nan_host = 0;
     TK_TRY(cudaMemcpyAsync(&nan_host, nan_flag, sizeof(int), cudaMemcpyDeviceToHost, s));

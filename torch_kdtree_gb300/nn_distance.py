@@ -35,6 +35,7 @@ gpu_available = bool(torch.cuda.is_available() and LIB.tk_cuda_available())
 _DTYPES = {torch.float32: _lib.TK_F32, torch.float64: _lib.TK_F64}
 MAX_LEVELS = 24
 MAX_K = 128
+MAX_DIMS = 8  # KD-tree dimensions (1-3 as the reference compiles, 4-8 as its README recipe adds)
 
 
 def default_levels(n: int) -> int:
@@ -109,7 +110,7 @@ class TorchKDTree:
         if points_ref.shape[0] >= 2 ** 31:
             raise AssertionError("Only 32 bit signed indexing implemented")
         dtype, dims = points_ref.dtype, points_ref.shape[-1]
-        if points_ref.dim() != 2 or dtype not in _DTYPES or dims not in (1, 2, 3):
+        if points_ref.dim() != 2 or dtype not in _DTYPES or not 1 <= dims <= MAX_DIMS:
             raise RuntimeError(
                 "Could not find the KD-Tree for your specified options. This probably means the library was not "
                 f"compiled for the specified dimensionality ({dims}) or precision ({dtype}).")
