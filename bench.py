@@ -353,10 +353,8 @@ def run_ours(args, rank, world):
     d_host = torch.empty(nq, K_NN).pin_memory()
     i_host = torch.empty(nq, K_NN, dtype=torch.int32).pin_memory()
 
-    def step_e2e():
-        dd, ii = chosen.query(q_host, nr_nns_searches=K_NN)
-        d_host.copy_(dd, non_blocking=True)
-        i_host.copy_(ii, non_blocking=True)
+    def step_e2e():  # one host-buffer query (tk_tree_query_host): copies pipelined with the search
+        chosen.query(q_host, nr_nns_searches=K_NN, result_dists=d_host, result_idx=i_host)
 
     ms_e2e = timed(step_e2e, args.steps, args.warmup)
 
@@ -411,6 +409,8 @@ def run_ours(args, rank, world):
         "e2e": {"value": world * nq * args.steps / (t_e2e / 1e3), "unit": UNIT,
                 "h2d_bytes_per_step": q_host.numel() * 4,
                 "d2h_bytes_per_step": d_host.numel() * 4 + i_host.numel() * 4,
+                "transfer": "tk_tree_query_host: queries in one H2D copy; results written by the query kernel "
+                            "straight into the pinned host buffers",
                 "ms_per_step": t_e2e / args.steps},
         "gpu_launches": 4 * args.steps,
         "clocks": clocks,
@@ -684,6 +684,64 @@ def run_plain(args):
     print(json.dumps(line), flush=True)
 
 
+def run_wide(args):
+    """KD trees of 4, 6 and 8 dimensions (the reference's README recipe for more
+    dims): 1,048,576 refs and 262,144 queries N(0,1), k=16, float32; tuned tree
+    depth and lanes.  Beside it: the exhaustive exact search on the same
+    queries, and the reference's CPU query (oracle restatement, all host
+    threads) on the first 16,384 queries, checked for exactness."""
+    import numpy as np
+    import torch
+
+    import torch_kdtree_gb300 as tk
+    from oracle import oracle as O
+    from torch_kdtree_gb300.autotune import autotune
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    O.build()
+    threads = os.cpu_count() or 1
+    n, nq, k, sample = 1 << 20, 1 << 18, 16, 16384
+    runs = {}
+    for d in (4, 6, 8):
+        rng = np.random.default_rng(40 + d)
+        ref_np = rng.standard_normal((n, d)).astype(np.float32)
+        q_np = rng.standard_normal((nq, d)).astype(np.float32)
+        ref, q = torch.from_numpy(ref_np).to(dev), torch.from_numpy(q_np).to(dev)
+        ch = autotune(ref, q, k, use_cache=False, max_queries=65536)
+        tree = tk.build_kd_tree(ref, levels=ch.levels, query_opts=ch.opts())
+        ms = _event_ms(lambda: tree.query(q, nr_nns_searches=k), args.steps, args.warmup)
+        kd_t = sum(ms) / len(ms) / 1e3
+        bq = q[:65536]
+        bms = _event_ms(lambda: tk.nn_distance(ref, bq, k), max(1, args.steps // 2), 1)
+        brute_qps = len(bq) / (sum(bms) / len(bms) / 1e3)
+        gd, gi = tree.query(q[:sample], nr_nns_searches=k)
+        lay = O.build_tree(ref_np, O.default_levels(n), nthreads=threads)
+        t0 = time.perf_counter()
+        od, oi = O.query_tree(lay, q_np[:sample], k, nthreads=threads)
+        cpu_t = time.perf_counter() - t0
+        cmp = O.compare_knn(od, oi, gd.cpu().numpy(), gi.cpu().numpy())
+        runs[f"d{d}"] = {"queries_per_s": nq / kd_t, "ms": 1e3 * kd_t, "levels": ch.levels,
+                         "threads_per_query": ch.threads_per_query, "prune_boxes": ch.prune_boxes,
+                         "brute_exact_queries_per_s": brute_qps,
+                         "cpu_reference_queries_per_s": sample / cpu_t,
+                         "cpu_reference_levels": O.default_levels(n),
+                         "exact_vs_cpu": {"index_mismatches_non_tie": cmp.mismatches,
+                                          "tie_queries": cmp.tie_queries,
+                                          "dist_bit_mismatches": cmp.dist_bit_mismatch}}
+        del tree, ref, q
+    line = {
+        "metric": "KNN queries/s, KD trees of 4-8 dims (1,048,576 refs x 262,144 queries N(0,1), k=16); value = d=6",
+        "value": runs["d6"]["queries_per_s"], "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": runs["d6"]["ms"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded numpy)",
+        "config": {"workload": "KD query, d in {4, 6, 8}, tuned depth and lanes, inputs resident"},
+        "cpu_baseline": {"value": runs["d6"]["cpu_reference_queries_per_s"], "unit": UNIT, "cores": threads,
+                         "kind": "port", "sample": f"first {sample} queries, reference default depth"},
+        "runs": runs,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_brute_tc(args):
     """Tensor-core brute force vs the FP32 CUDA-core brute force: 262,144 refs,
     65,536 queries, N(0,1) in d = 8 and 32 with 5% exact duplicate refs, k=32.
@@ -757,7 +815,7 @@ def main():
                    help="chosen: 1 = per-query stacks, 2 = warp packets (with --levels/--tpq)")
     p.add_argument("--profile", action="store_true", help="run one chosen and one plain query only (for ncu)")
     p.add_argument("--workload", default="kd",
-                   choices=["kd", "plain", "readme", "batched", "backward", "brute", "brute_tc"],
+                   choices=["kd", "plain", "readme", "batched", "backward", "brute", "brute_tc", "wide"],
                    help="kd (default): the headline large single-cloud query; the others measure the "
                         "batched, backward and brute-force paths")
     p.add_argument("--leaf-size", type=int, default=16, help="target points per leaf of tuned batch trees")
@@ -773,7 +831,7 @@ def main():
         if rank == 0:
             {"plain": run_plain, "readme": run_readme, "batched": run_batched, "backward": run_backward,
              "brute": run_brute,
-             "brute_tc": run_brute_tc}[args.workload](args)
+             "brute_tc": run_brute_tc, "wide": run_wide}[args.workload](args)
         return
     if world > 1:
         import torch

@@ -59,8 +59,9 @@ typedef struct tk_tree_info {
 } tk_tree_info;
 
 /* Build a KD-tree on the host in the reference's layout and upload it.
- * host_points: [n, dims] C-contiguous, float or double per dtype.
- * levels: 1..24 (the reference's default heuristic is applied by the Python
+ * host_points: [n, dims] C-contiguous, float or double per dtype; dims
+ * 1..8 (1-3 as the reference compiles, 4-8 as its README's extra template
+ * instantiations add).  levels: 1..24 (the reference's default heuristic is applied by the Python
  * layer).  device: CUDA ordinal, or -1 for a host-only tree (layout getters
  * only; queries on it fail with TK_EINVAL).  n_threads: host build threads
  * (0 = all hardware threads).  Fails with TK_EINVAL when a split node would receive no point
@@ -143,6 +144,28 @@ size_t tk_tree_query_workspace_size(const tk_tree* tree, int64_t nq);
 int tk_tree_query(const tk_tree* tree, const void* q, int64_t nq, int k, void* dists, int32_t* idx,
                   const tk_query_opts* opts, void* workspace, size_t workspace_bytes, void* stream);
 
+/* Transfers of tk_tree_query_host. */
+#define TK_HOST_AUTO 0   /* direct when both result buffers are registered host memory, else staged */
+#define TK_HOST_DIRECT 1 /* the query kernel writes the results into the host buffers itself */
+#define TK_HOST_STAGED 2 /* results to device staging, downloaded after the search */
+
+/* Exact k nearest neighbours with the queries and results in HOST memory:
+ * q host [nq, dims] (tree dtype), dists host [nq, k], idx host int32
+ * [nq, k].  The queries are uploaded into device staging with one copy.
+ * When the result buffers are registered (pinned: cudaHostAlloc /
+ * cudaHostRegister) memory the GPU addresses, the query kernel writes the
+ * results straight into them over the host link while it searches
+ * (TK_HOST_DIRECT; TK_EINVAL when they are not registered); otherwise they
+ * are downloaded from device staging after the search (TK_HOST_STAGED).
+ * Synchronous on `stream`: returns when the results are in host memory.
+ * Device staging and workspace are allocated on first use and kept, grown as
+ * needed, until tk_tree_destroy; calls on one tree are serialised.  Results
+ * are identical to tk_tree_query's.  Replaces the host-tensor use of
+ * TorchKDTree.query (torch_kdtree/nn_distance.py:80 copies the queries to
+ * the device; the caller copies the results back). */
+int tk_tree_query_host(const tk_tree* tree, const void* q, int64_t nq, int k, void* dists, int32_t* idx,
+                       const tk_query_opts* opts, int transfer, void* stream);
+
 /* Largest query count tk_tree_query_noalloc accepts in one call. */
 #define TK_NOALLOC_MAX_QUERIES 262144
 
@@ -167,7 +190,8 @@ int tk_tree_query_noalloc(const tk_tree* tree, const void* q, int64_t nq, int k,
 typedef struct tk_batch tk_batch;
 
 /* Plan a batched query over n_trees clouds, each with its own tree (same
- * dtype, dims and device) and its own k (ks[c], 1..min(n_c, 128)); query
+ * dtype, dims and device; dims 1..3 -- wider trees are queried one by one)
+ * and its own k (ks[c], 1..min(n_c, 128)); query
  * counts per cloud are fixed by q_counts.  The trees must outlive the batch.
  * Queries are passed concatenated cloud after cloud ([sum q_counts, dims]);
  * results come back concatenated the same way, cloud c occupying a

@@ -12,6 +12,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libtkknn.so")
 
 TK_OK = 0
+TK_HOST_AUTO, TK_HOST_DIRECT, TK_HOST_STAGED = 0, 1, 2  # tk_tree_query_host transfers
 TK_EINVAL = 1
 TK_ENOMEM = 2
 TK_EUNSUPPORTED = 3
@@ -89,6 +90,7 @@ SIGNATURES = {
     "tk_nn_distance_workspace_size": (_sz, [_i64, _i64, _int, _int, _int, _int]),
     "tk_nn_distance": (_int, [_vp, _i64, _vp, _i64, _int, _int, _int, _int, _vp, _vp, _vp, _sz, _vp]),
     "tk_tree_query_noalloc": (_int, [_vp, _vp, _i64, _int, _vp, _vp, ctypes.POINTER(QueryOpts), _vp]),
+    "tk_tree_query_host": (_int, [_vp, _vp, _i64, _int, _vp, _vp, ctypes.POINTER(QueryOpts), _int, _vp]),
     "tk_knn_backward_workspace_size": (_sz, [_i64, _int, _i64]),
     "tk_knn_backward": (_int, [_vp, _vp, _vp, _vp, _i64, _i64, _int, _int, _int, _vp, _vp, _vp, _sz, _vp]),
 }

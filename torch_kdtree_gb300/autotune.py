@@ -105,8 +105,11 @@ def autotune(points_ref: torch.Tensor, queries: torch.Tensor, k: int,
             tree = build_kd_tree(points_ref, levels=L)
         except Exception:  # too deep for this cloud
             continue
-        cands = [(g, boxes, 1) for g in lanes if g * 16 >= k for boxes in (1, 0)]  # a lane holds <= 16 keys
-        if k <= 16:
+        # a lane holds <= 16 keys; trees of more than 3 dims run 1 or 32 lanes per
+        # query and the per-query-stack traversal only
+        shapes = [g for g in lanes if g * 16 >= k and (d <= 3 or g in (1, 32))]
+        cands = [(g, boxes, 1) for g in shapes for boxes in (1, 0)]
+        if k <= 16 and d <= 3:
             cands.append((1, 1, 2))  # warp packets
         for g, boxes, trav in cands:
             ms = time_query(tree, q, k, QueryOpts.make(threads_per_query=g, prune_boxes=boxes, traversal=trav), reps)

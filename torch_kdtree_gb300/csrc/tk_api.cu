@@ -243,8 +243,8 @@ int run_query_wide(const tk_tree* t, const T* q, int nq, int k, T* dists, int32_
     int G = o.threads_per_query > 0 ? o.threads_per_query : auto_lanes(t, nq, k);
     if (G != 1 && G != 2 && G != 4 && G != 8 && G != 16 && G != 32)
         return fail(TK_EINVAL, "threads_per_query must be 1, 2, 4, 8, 16 or 32");
-    if (G != 1 || k > 16) G = 32;  // kernels of wide trees: 1 or 32 lanes per query
-    const int R = G == 1 ? pow2_ceil(k) : pow2_ceil((k + 31) / 32);
+    if (G != 1 || k > 16) G = 32;  // kernels of wide trees: 1 (k <= 16) or 32 lanes per query
+    const int R = pow2_ceil((k + G - 1) / G);
     const int W = record_width(t->dims);
     const int L = t->levels;
     int S = o.smem_levels >= 0 ? o.smem_levels : 10;
@@ -602,6 +602,8 @@ int tk_tree_destroy(tk_tree* t) {
     if (t->device >= 0) {
         DeviceGuard g(t->device);
         free_tree_device(t);
+        tk::free_host_pipe(t->pipe);
+        t->pipe = nullptr;
     }
     delete t;
     return TK_OK;
@@ -795,4 +797,127 @@ extern "C" int tk_tree_query_noalloc(const tk_tree* t, const void* q, int64_t nq
         case 3: return run_query<double, 3>(t, qq, n32, k, dd, idx, o, ws, s);
         default: return run_query_wide<double>(t, qq, n32, k, dd, idx, o, ws, s);
     }
+}
+
+// ------------------------------------------------- host-buffer query --
+//
+// tk_tree_query_host: queries and results in host memory.  The queries are
+// uploaded into device staging with one copy (the search reads each query
+// more than once; host reads at link latency slowed it down), then:
+//  * direct: the result buffers are registered (pinned) memory that the GPU
+//    can address, so the query kernel writes the results into host memory
+//    itself (over NVLink-C2C on Grace-Blackwell), spread over the search
+//    instead of a download after it;
+//  * staged: the results go to device staging and are downloaded after the
+//    search.
+// Device staging and workspace are kept per tree (grown as needed) and freed
+// with it; calls on one tree are serialised by its mutex.
+
+namespace tk {
+
+struct HostPipe {
+    std::mutex mu;
+    char* buf = nullptr;
+    size_t cap = 0;
+};
+
+void free_host_pipe(HostPipe* p) {
+    if (!p) return;
+    if (p->buf) cudaFree(p->buf);
+    delete p;
+}
+
+namespace {
+
+std::mutex g_pipe_create_mu;
+
+HostPipe* host_pipe(const tk_tree* t) {
+    std::lock_guard<std::mutex> lk(g_pipe_create_mu);
+    if (!t->pipe) t->pipe = new HostPipe();
+    return t->pipe;
+}
+
+// Device address of registered host memory, or null when the GPU cannot
+// address it (pageable memory, or not host memory at all).
+void* mapped_host(const void* p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
+int pipe_buffer(HostPipe* p, size_t need, char** out) {
+    if (p->cap < need) {
+        if (p->buf) cudaFree(p->buf);
+        p->buf = nullptr;
+        p->cap = 0;
+        const cudaError_t e = cudaMalloc(&p->buf, need);
+        if (e != cudaSuccess) return fail(TK_ECUDA, std::string("host query staging: ") + cudaGetErrorString(e));
+        p->cap = need;
+    }
+    *out = p->buf;
+    return TK_OK;
+}
+
+}  // namespace
+}  // namespace tk
+
+extern "C" int tk_tree_query_host(const tk_tree* t, const void* q, int64_t nq, int k, void* dists, int32_t* idx,
+                                  const tk_query_opts* opts, int transfer, void* stream) {
+    using namespace tk;
+    clear_error();
+    if (!t) return fail(TK_EINVAL, "tree is null");
+    if (nq < 0 || nq >= (int64_t(1) << 31)) return fail(TK_EINVAL, "number of queries must be in [0, 2^31)");
+    if (k < 1) return fail(TK_EINVAL, "k must be >= 1");
+    if (k > t->n) return fail(TK_EINVAL, "You requested more nearest neighbors than there are in the KD-Tree");
+    if (k > kMaxK) return fail(TK_EINVAL, "k is limited to 128 on the GPU");
+    if (t->device < 0 || !t->d_pts) return fail(TK_EINVAL, "tree was built host-only (device < 0); it has no device image");
+    if (transfer != TK_HOST_AUTO && transfer != TK_HOST_DIRECT && transfer != TK_HOST_STAGED)
+        return fail(TK_EINVAL, "transfer must be TK_HOST_AUTO, TK_HOST_DIRECT or TK_HOST_STAGED");
+    if (nq == 0) return TK_OK;
+    if (!q || !dists || !idx) return fail(TK_EINVAL, "null query or output pointer");
+
+    DeviceGuard g(t->device);
+    void* md = nullptr;
+    void* mi = nullptr;
+    if (transfer != TK_HOST_STAGED) {
+        md = mapped_host(dists);
+        mi = mapped_host(idx);
+    }
+    const bool direct = md && mi;
+    if (transfer == TK_HOST_DIRECT && !direct)
+        return fail(TK_EINVAL, "direct transfer needs registered (pinned) result buffers the GPU can address");
+
+    HostPipe* p = host_pipe(t);
+    std::lock_guard<std::mutex> lk(p->mu);
+    const size_t es = t->dtype == TK_F32 ? 4 : 8;
+    const size_t qb = es * size_t(t->dims) * size_t(nq), db = es * size_t(k) * size_t(nq),
+                 ib = 4 * size_t(k) * size_t(nq);
+    const size_t wsb = align_up(ws_layout(t->levels, nq).total, 256);
+    const size_t need = wsb + align_up(qb, 256) + (direct ? 0 : align_up(db, 256) + align_up(ib, 256));
+    char* buf = nullptr;
+    int rc = pipe_buffer(p, need, &buf);
+    if (rc != TK_OK) return rc;
+    tk_query_opts o{0, -1, -1, 0, 0, nullptr, nullptr, -1, 0};
+    if (opts) o = *opts;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    cudaError_t e = cudaSuccess;
+    char* dq = buf + wsb;
+    e = cudaMemcpyAsync(dq, q, qb, cudaMemcpyHostToDevice, s);
+    if (direct) {
+        if (e == cudaSuccess) rc = tk_tree_query(t, dq, nq, k, md, static_cast<int32_t*>(mi), &o, buf, wsb, s);
+    } else {
+        char* dd = dq + align_up(qb, 256);
+        char* di = dd + align_up(db, 256);
+        if (e == cudaSuccess) rc = tk_tree_query(t, dq, nq, k, dd, reinterpret_cast<int32_t*>(di), &o, buf, wsb, s);
+        if (e == cudaSuccess && rc == TK_OK) e = cudaMemcpyAsync(dists, dd, db, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess && rc == TK_OK) e = cudaMemcpyAsync(idx, di, ib, cudaMemcpyDeviceToHost, s);
+    }
+    const cudaError_t se = cudaStreamSynchronize(s);  // whatever was queued completes, also on failure
+    if (rc != TK_OK) return rc;
+    if (e == cudaSuccess) e = se;
+    if (e != cudaSuccess) return fail(TK_ECUDA, std::string("host query: ") + cudaGetErrorString(e));
+    return TK_OK;
 }

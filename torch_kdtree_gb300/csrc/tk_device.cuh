@@ -210,6 +210,27 @@ struct TopK {
 
     // Write the k live slots of this lane to row `row` of the outputs.
     __device__ __forceinline__ void store(int k, int gl, T* out_d, int32_t* out_i, long long row) const {
+        if constexpr (G == 1 && R % 4 == 0) {
+            // all R slots live and both rows 16-byte aligned: 16-byte stores
+            T* pd = out_d + row * k;
+            int32_t* pi = out_i + row * k;
+            if (k == R && ((reinterpret_cast<uintptr_t>(pd) | reinterpret_cast<uintptr_t>(pi)) & 15) == 0) {
+#pragma unroll
+                for (int r = 0; r < R; r += 4) {
+                    if constexpr (sizeof(T) == 4) {
+                        *reinterpret_cast<float4*>(pd + r) =
+                            make_float4(slot[r].dist(), slot[r + 1].dist(), slot[r + 2].dist(), slot[r + 3].dist());
+                    } else {
+                        *reinterpret_cast<double2*>(pd + r) = make_double2(slot[r].dist(), slot[r + 1].dist());
+                        *reinterpret_cast<double2*>(pd + r + 2) = make_double2(slot[r + 2].dist(), slot[r + 3].dist());
+                    }
+                    *reinterpret_cast<int4*>(pi + r) =
+                        make_int4(int32_t(slot[r].index()), int32_t(slot[r + 1].index()), int32_t(slot[r + 2].index()),
+                                  int32_t(slot[r + 3].index()));
+                }
+                return;
+            }
+        }
 #pragma unroll
         for (int r = 0; r < R; ++r) {
             const int s = r * G + gl;

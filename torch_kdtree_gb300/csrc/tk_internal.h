@@ -58,6 +58,10 @@ int tree_from_layout(const T* structured, const int32_t* perm, const T* medians,
 struct tk_tree;
 
 namespace tk {
+// Streams, events and device staging of tk_tree_query_host (tk_api.cu),
+// created on a tree's first host-buffer query.
+struct HostPipe;
+void free_host_pipe(HostPipe* p);
 // Builds the tree on the GPU from device points straight into t's device
 // image (tree_build_gpu.cu), same layout as build_host_tree.  The arguments
 // are validated by the caller; runs on and synchronises the CUDA stream
@@ -86,4 +90,5 @@ struct tk_tree {
     void* d_boxes = nullptr;     // per node {lo.xyz, 0}, {hi.xyz, 0} (see tk_device.cuh); lo / hi rows when wide
     int32_t* d_perm = nullptr;   // trees of 4-8 dims: original index of each point (records hold coordinates only)
     int64_t device_bytes = 0;
+    mutable tk::HostPipe* pipe = nullptr;  // host-buffer query resources (see tk_tree_query_host)
 };

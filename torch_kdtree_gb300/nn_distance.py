@@ -99,6 +99,16 @@ def knn_query_raw(tree: _Tree, q: torch.Tensor, k: int, dists: torch.Tensor, idx
                             _stream_ptr(q.device)))
 
 
+def knn_query_host(tree: _Tree, q: torch.Tensor, k: int, dists: torch.Tensor, idx: torch.Tensor, device: torch.device,
+                   opts: Optional[QueryOpts] = None, transfer: int = _lib.TK_HOST_AUTO) -> None:
+    """One tk_tree_query_host: queries and results in host memory; the query
+    kernel writes pinned result buffers directly, others are downloaded from
+    device staging.  Returns when the results are on the host."""
+    check(LIB.tk_tree_query_host(tree.handle, q.data_ptr(), q.shape[0], k, dists.data_ptr(), idx.data_ptr(),
+                                 ctypes.byref(opts) if opts is not None else None, int(transfer),
+                                 _stream_ptr(device)))
+
+
 class TorchKDTree:
     def __init__(self, points_ref: torch.Tensor, device: torch.device, levels: int, squared_distances: bool,
                  query_opts: Optional[QueryOpts] = None, build: str = "auto"):
@@ -187,7 +197,13 @@ class TorchKDTree:
         Returns ``(dists, inds)``: squared (or, with ``squared_distances=False``,
         plain) distances ``[Q, k]`` in the tree's dtype and int32 original
         indices ``[Q, k]``.  Raises RuntimeError when k exceeds the number of
-        points, AssertionError on dtype / shape mismatches, as the reference."""
+        points, AssertionError on dtype / shape mismatches, as the reference.
+
+        ``result_dists`` / ``result_idx`` may also be CPU tensors (the
+        reference takes device buffers only): the results are then written
+        there and returned on the CPU.  With CPU queries as well (and no
+        gradient), the query is one tk_tree_query_host call: with pinned
+        result tensors the query kernel writes them directly."""
         k = int(nr_nns_searches)
         if k > self.nr_ref_points:
             raise RuntimeError("You requested more nearest neighbors than there are in the KD-Tree")
@@ -195,20 +211,23 @@ class TorchKDTree:
             raise RuntimeError("nr_nns_searches must be at least 1")
         if k > MAX_K:
             raise RuntimeError(f"nr_nns_searches is limited to {MAX_K} on the GPU")
+        host_out = (result_dists is not None and result_idx is not None and result_dists.device.type == "cpu"
+                    and result_idx.device.type == "cpu")
+        need_grad = torch.is_grad_enabled() and (points_query.requires_grad or self.ref_requires_grad)
+        if host_out and points_query.device.type == "cpu" and not need_grad:
+            return self._query_host(points_query, k, result_dists, result_idx)
+        out_d = out_i = None
+        if host_out:
+            self._check_query(points_query, k, result_dists, result_idx)
+            out_d, out_i = result_dists, result_idx
+            result_dists = result_idx = None
         points_query = points_query.to(self.device)
         nq = points_query.shape[0]
         if result_dists is None:
             result_dists = torch.empty((nq, k), dtype=self.dtype, device=self.device)
         if result_idx is None:
             result_idx = torch.empty((nq, k), dtype=self.dtype_idx, device=self.device)
-        if list(result_dists.shape) != [nq, k] or result_dists.dtype != self.dtype:
-            raise AssertionError("result_dists must be [Q, k] of the tree's dtype")
-        if list(result_idx.shape) != [nq, k] or result_idx.dtype != self.dtype_idx:
-            raise AssertionError("result_idx must be [Q, k] int32")
-        if points_query.dtype != self.dtype:
-            raise AssertionError(f"points_query has dtype {points_query.dtype}, the tree {self.dtype}")
-        if points_query.dim() != 2 or points_query.shape[1] != self.dims:
-            raise AssertionError(f"points_query must be [Q, {self.dims}]")
+        self._check_query(points_query, k, result_dists, result_idx)
         if not result_dists.is_contiguous():
             result_dists = result_dists.contiguous()
         if not result_idx.is_contiguous():
@@ -227,9 +246,42 @@ class TorchKDTree:
         else:
             knn_query_raw(self._tree, points_query.detach(), k, result_dists, result_idx, self.query_opts)
             dists, inds = result_dists, result_idx
+        if out_d is not None:  # CPU result buffers with device queries or a gradient
+            with torch.no_grad():
+                out_d.copy_(result_dists)
+                out_i.copy_(result_idx)
+            dists = out_d if dists is result_dists else dists.to("cpu")
+            inds = out_i
         if not self.squared_distances:
             dists = torch.sqrt(dists)
         return dists, inds
+
+    def _check_query(self, points_query: torch.Tensor, k: int, result_dists: torch.Tensor,
+                     result_idx: torch.Tensor) -> None:
+        nq = points_query.shape[0]
+        if list(result_dists.shape) != [nq, k] or result_dists.dtype != self.dtype:
+            raise AssertionError("result_dists must be [Q, k] of the tree's dtype")
+        if list(result_idx.shape) != [nq, k] or result_idx.dtype != self.dtype_idx:
+            raise AssertionError("result_idx must be [Q, k] int32")
+        if points_query.dtype != self.dtype:
+            raise AssertionError(f"points_query has dtype {points_query.dtype}, the tree {self.dtype}")
+        if points_query.dim() != 2 or points_query.shape[1] != self.dims:
+            raise AssertionError(f"points_query must be [Q, {self.dims}]")
+
+    def _query_host(self, points_query: torch.Tensor, k: int, result_dists: torch.Tensor,
+                    result_idx: torch.Tensor):
+        """CPU queries into CPU result buffers through tk_tree_query_host."""
+        self._check_query(points_query, k, result_dists, result_idx)
+        q = points_query.detach().contiguous()
+        if not result_dists.is_contiguous():
+            result_dists = result_dists.contiguous()
+        if not result_idx.is_contiguous():
+            result_idx = result_idx.contiguous()
+        knn_query_host(self._tree, q, k, result_dists, result_idx, self.device, self.query_opts)
+        dists = result_dists
+        if not self.squared_distances:
+            dists = torch.sqrt(dists)
+        return dists, result_idx
 
 
 def build_kd_tree(points_ref: Union[torch.Tensor, np.ndarray], device: Optional[torch.device] = None,
