@@ -65,6 +65,24 @@ def test_noalloc_matches_workspace_query_twice():
         LIB.tk_tree_destroy(h)
 
 
+@pytest.mark.parametrize("dims", [2, 5, 8])
+def test_noalloc_other_dimensions(dims):
+    """Trees of 1-2 and 4-8 dimensions go through the same static scratch."""
+    from torch_kdtree_gb300._lib import LIB
+    rng = np.random.default_rng(dims)
+    pts = rng.standard_normal((50_000, dims)).astype(np.float32)
+    h = _tree(LIB, pts, 11)
+    try:
+        q = torch.from_numpy(rng.standard_normal((40_000, dims)).astype(np.float32)).cuda()
+        d_ref, i_ref = _query_with_workspace(LIB, h, q, 12)
+        d, i = _query_noalloc(LIB, h, q, 12)
+        torch.cuda.synchronize()
+        assert torch.equal(d, d_ref)
+        assert torch.equal(i, i_ref)
+    finally:
+        LIB.tk_tree_destroy(h)
+
+
 def test_noalloc_rejects_oversize_requests():
     from torch_kdtree_gb300._lib import LIB, TK_EINVAL, TK_NOALLOC_MAX_QUERIES
     pts = np.random.default_rng(1).random((1000, 3)).astype(np.float32)
