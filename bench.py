@@ -698,9 +698,18 @@ def run_wide(args):
     from torch_kdtree_gb300.autotune import autotune
     dev = torch.device("cuda", 0)
     torch.cuda.set_device(dev)
+    n, nq, k, sample = 1 << 20, 1 << 18, 16, 16384
+    if args.profile:  # one d=8 query of 65,536 queries, tuned shape (levels 12, 32 lanes, split planes only)
+        from torch_kdtree_gb300._lib import QueryOpts
+        rng = np.random.default_rng(48)
+        ref = torch.from_numpy(rng.standard_normal((n, 8)).astype(np.float32)).to(dev)
+        q = torch.from_numpy(rng.standard_normal((65536, 8)).astype(np.float32)).to(dev)
+        tree = tk.build_kd_tree(ref, levels=12, query_opts=QueryOpts.make(threads_per_query=32, prune_boxes=0))
+        tree.query(q, nr_nns_searches=k)
+        torch.cuda.synchronize()
+        return
     O.build()
     threads = os.cpu_count() or 1
-    n, nq, k, sample = 1 << 20, 1 << 18, 16, 16384
     runs = {}
     for d in (4, 6, 8):
         rng = np.random.default_rng(40 + d)
