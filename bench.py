@@ -412,7 +412,10 @@ def run_ours(args, rank, world):
                 "transfer": "tk_tree_query_host: queries in one H2D copy; results written by the query kernel "
                             "straight into the pinned host buffers",
                 "ms_per_step": t_e2e / args.steps},
-        "gpu_launches": 4 * args.steps,
+        # per chosen step (one graph replay): k_bin_count, the three kernels of the
+        # cell-count scan (k_scan_tiles, k_scan_single, k_scan_add), k_bin_scatter
+        # and the KD query kernel
+        "gpu_launches": 6 * args.steps,
         "clocks": clocks,
     }
     print(json.dumps(line), flush=True)
