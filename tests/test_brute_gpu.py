@@ -141,3 +141,42 @@ def test_auto_mode_picks_a_mode_and_stays_exact(tmp_path, monkeypatch, oracle):
         np.testing.assert_array_equal(ii.cpu().numpy(), bi)
     import json
     assert len(json.load(open(tmp_path / "cache.json"))) == 3
+
+
+@pytest.mark.parametrize("mode", ["exact", "tf32", "bf16_split"])
+def test_infinite_and_overflowing_queries(mode, oracle):
+    """Rows whose distances are +inf to every reference (infinite coordinates,
+    or squares that overflow) tie at +inf: the k lowest indices, in every mode
+    (the tensor-core modes cannot certify them and fall back to exact)."""
+    rng = np.random.default_rng(77)
+    ref = rng.standard_normal((20000, 8)).astype(np.float32)
+    q = rng.standard_normal((600, 8)).astype(np.float32)
+    q[3, 0] = np.inf
+    q[4, 0] = -np.inf
+    q[5, :] = 1e20
+    q[6, 0], q[6, 1] = np.inf, -np.inf
+    q[7, 0] = 3e19
+    dd, ii = tk().nn_distance(torch.from_numpy(ref).to(cuda), torch.from_numpy(q).to(cuda), 5, mode=mode)
+    bd, bi = oracle.brute(ref, q, 5)
+    assert np.isinf(bd[3:8]).all() and (bi[3:8] == np.arange(5)).all()
+    np.testing.assert_array_equal(dd.cpu().numpy(), bd)
+    np.testing.assert_array_equal(ii.cpu().numpy(), bi)
+
+
+@pytest.mark.parametrize("mode", ["exact", "tf32", "bf16_split"])
+def test_infinite_and_huge_references(mode, oracle):
+    """References with infinite coordinates or norms beyond the tensor-core
+    range: the tensor-core modes certify nothing and fall back to exact; the
+    answers equal the oracle's (such references sit at distance +inf)."""
+    rng = np.random.default_rng(78)
+    ref = rng.standard_normal((20000, 8)).astype(np.float32)
+    ref[5, 2] = np.inf
+    ref[9, 0] = -np.inf
+    ref[11, :] = 3e19
+    q = rng.standard_normal((700, 8)).astype(np.float32)
+    q[0, :] = 3e19  # next to ref 11: distance 0 there, +inf to everything else
+    dd, ii = tk().nn_distance(torch.from_numpy(ref).to(cuda), torch.from_numpy(q).to(cuda), 4, mode=mode)
+    bd, bi = oracle.brute(ref, q, 4)
+    assert bi[0, 0] == 11 and bd[0, 0] == 0
+    np.testing.assert_array_equal(dd.cpu().numpy(), bd)
+    np.testing.assert_array_equal(ii.cpu().numpy(), bi)

@@ -276,3 +276,48 @@ def test_wide_tree_build_save_load_and_grad(tmp_path, oracle):
     from torch_kdtree_gb300.batched import BatchedKDTrees
     with pytest.raises(Exception):
         BatchedKDTrees([rt], [4], [10])
+
+
+def _non_finite_rows(q):
+    """Rows whose distances are +inf to every point (infinite coordinates, or
+    squares that overflow): every candidate ties at +inf, so the answer is the
+    k lowest original indices."""
+    q[3, 0] = np.inf
+    q[4, 0] = -np.inf
+    q[5, :] = 1e20
+    q[6, 0], q[6, 1] = np.inf, -np.inf
+    q[7, 0] = 3e19
+    return q
+
+
+@pytest.mark.parametrize("dims", [3, 5])
+def test_infinite_and_overflowing_queries(dims, oracle):
+    rng = np.random.default_rng(70 + dims)
+    ref = rng.standard_normal((5000, dims)).astype(np.float32)
+    q = _non_finite_rows(rng.standard_normal((400, dims)).astype(np.float32))
+    bd, bi = oracle.brute(ref, q, 6)
+    assert np.isinf(bd[3:8]).all() and (bi[3:8] == np.arange(6)).all()
+    shapes = [dict(), dict(threads_per_query=1), dict(threads_per_query=32), dict(threads_per_query=1, prune_boxes=0)]
+    if dims == 3:
+        shapes.append(dict(traversal=2))
+    for opts in shapes:
+        d, i = gpu_query(ref, q, 6, levels=8, **opts)
+        np.testing.assert_array_equal(d, bd, err_msg=str(opts))
+        np.testing.assert_array_equal(i, bi, err_msg=str(opts))
+
+
+@pytest.mark.parametrize("dims", [3, 6])
+def test_infinite_and_huge_reference_points(dims, oracle):
+    rng = np.random.default_rng(80 + dims)
+    ref = rng.standard_normal((4000, dims)).astype(np.float32)
+    ref[5, 0] = np.inf
+    ref[9, 1] = -np.inf
+    ref[11, :] = 3e19
+    q = rng.standard_normal((300, dims)).astype(np.float32)
+    q[0, :] = 3e19
+    bd, bi = oracle.brute(ref, q, 5)
+    assert bi[0, 0] == 11 and bd[0, 0] == 0
+    for opts in (dict(), dict(threads_per_query=1), dict(threads_per_query=32, prune_boxes=0)):
+        d, i = gpu_query(ref, q, 5, levels=7, **opts)
+        np.testing.assert_array_equal(d, bd, err_msg=str(opts))
+        np.testing.assert_array_equal(i, bi, err_msg=str(opts))

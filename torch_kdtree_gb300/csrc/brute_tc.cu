@@ -130,6 +130,7 @@ int run_brute_tc(const float* ref, int64_t n, const float* q, int64_t nq, int d,
     char* p = static_cast<char*>(ws);
     const int n32 = int(n), nq32 = int(nq);
     cudaError_t e0 = cudaMemsetAsync(p + w.err, 0, sizeof(int), s);
+    int* err = reinterpret_cast<int*>(p + w.err);  // no certificates when set (see kTcNormLimit)
     if (e0 != cudaSuccess) return fail(TK_ECUDA, std::string("memset: ") + cudaGetErrorString(e0));
     int crc = TK_OK;
     if (w.tc5) {
@@ -142,13 +143,15 @@ int run_brute_tc(const float* ref, int64_t n, const float* q, int64_t nq, int d,
         unsigned char* blo = reinterpret_cast<unsigned char*>(p + w.b_lo);
         const int nq_pad = qblocks * kT5Rows;
         if (mode == TK_BRUTE_TF32) {
-            k_tc5_pack<TK_BRUTE_TF32><<<(nq_pad + 255) / 256, 256, 0, s>>>(q, nq32, nq_pad, d, w.KP, kT5Rows, 1, ahi, alo);
-            k_tc5_pack<TK_BRUTE_TF32><<<(n_pad + 255) / 256, 256, 0, s>>>(ref, n32, n_pad, d, w.KP, kT5Cols, 0, bhi, blo);
+            k_tc5_pack<TK_BRUTE_TF32><<<(nq_pad + 255) / 256, 256, 0, s>>>(q, nq32, nq_pad, d, w.KP, kT5Rows, 1, ahi, alo,
+                                                                         err);
+            k_tc5_pack<TK_BRUTE_TF32><<<(n_pad + 255) / 256, 256, 0, s>>>(ref, n32, n_pad, d, w.KP, kT5Cols, 0, bhi, blo,
+                                                                        err);
         } else {
             k_tc5_pack<TK_BRUTE_BF16_SPLIT><<<(nq_pad + 255) / 256, 256, 0, s>>>(q, nq32, nq_pad, d, w.KP, kT5Rows, 1,
-                                                                               ahi, alo);
+                                                                               ahi, alo, err);
             k_tc5_pack<TK_BRUTE_BF16_SPLIT><<<(n_pad + 255) / 256, 256, 0, s>>>(ref, n32, n_pad, d, w.KP, kT5Cols, 0,
-                                                                              bhi, blo);
+                                                                              bhi, blo, err);
         }
         Tc5Args t5{};
         t5.a_hi = ahi;
@@ -167,16 +170,18 @@ int run_brute_tc(const float* ref, int64_t n, const float* q, int64_t nq, int d,
         if (crc != TK_OK) return crc;
     } else if (mode == TK_BRUTE_TF32) {
         k_tc_pack<TK_BRUTE_TF32><<<(nq32 + 255) / 256, 256, 0, s>>>(q, nq32, d, w.KP, reinterpret_cast<uint32_t*>(p + w.a_pack),
-                                                                  nullptr, nullptr, reinterpret_cast<float*>(p + w.qnorm));
+                                                                  nullptr, nullptr, reinterpret_cast<float*>(p + w.qnorm),
+                                                                  nullptr);
         k_tc_pack<TK_BRUTE_TF32><<<(n32 + 255) / 256, 256, 0, s>>>(ref, n32, d, w.KP, reinterpret_cast<uint32_t*>(p + w.b_pack),
-                                                                 nullptr, nullptr, reinterpret_cast<float*>(p + w.rnorm));
+                                                                 nullptr, nullptr, reinterpret_cast<float*>(p + w.rnorm),
+                                                                 err);
     } else {
         k_tc_pack<TK_BRUTE_BF16_SPLIT><<<(nq32 + 255) / 256, 256, 0, s>>>(
             q, nq32, d, w.KP, nullptr, reinterpret_cast<__nv_bfloat16*>(p + w.a_pack),
-            reinterpret_cast<__nv_bfloat16*>(p + w.a_lo), reinterpret_cast<float*>(p + w.qnorm));
+            reinterpret_cast<__nv_bfloat16*>(p + w.a_lo), reinterpret_cast<float*>(p + w.qnorm), nullptr);
         k_tc_pack<TK_BRUTE_BF16_SPLIT><<<(n32 + 255) / 256, 256, 0, s>>>(
             ref, n32, d, w.KP, nullptr, reinterpret_cast<__nv_bfloat16*>(p + w.b_pack),
-            reinterpret_cast<__nv_bfloat16*>(p + w.b_lo), reinterpret_cast<float*>(p + w.rnorm));
+            reinterpret_cast<__nv_bfloat16*>(p + w.b_lo), reinterpret_cast<float*>(p + w.rnorm), err);
     }
     // 2. candidates
     TcArgs a{};

@@ -24,6 +24,16 @@ constexpr int kThreads = 256;
 
 inline size_t align256(size_t v) { return (v + 255) / 256 * 256; }
 
+// The certificate below reasons about finite scores: a slice whose list never
+// filled (tau = +inf) holds every reference of the slice.  NaN scores (from
+// non-finite coordinates) enter no list, and overflowing ones break the error
+// bound, so a query is certified only when |q|^2 < 2^125 and every reference
+// has |r|^2 < 2^125 (the pack kernel flags any other reference in `err`,
+// which certifies nothing).  Then every partial sum of a score is below
+// |r|^2 + 2|q||r| <= 2 (|q|^2 + |r|^2) < 2^127: finite.  Uncertified queries
+// are answered by the exact kernel.
+constexpr float kTcNormLimit = 0x1p125f;
+
 __device__ __forceinline__ uint32_t to_tf32(float x) {
     uint32_t r;
     asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
@@ -34,7 +44,8 @@ __device__ __forceinline__ uint32_t to_tf32(float x) {
 // hi and lo bf16 planes.  Rows are zero-padded to KP elements.
 template <int MODE>
 __global__ void k_tc_pack(const float* __restrict__ x, int rows, int d, int KP, uint32_t* __restrict__ tf,
-                          __nv_bfloat16* __restrict__ hi, __nv_bfloat16* __restrict__ lo, float* __restrict__ norm) {
+                          __nv_bfloat16* __restrict__ hi, __nv_bfloat16* __restrict__ lo, float* __restrict__ norm,
+                          int* __restrict__ err) {
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= rows) return;
     float s = 0.f;
@@ -50,6 +61,7 @@ __global__ void k_tc_pack(const float* __restrict__ x, int rows, int d, int KP, 
         }
     }
     norm[r] = s;
+    if (err && !(s < kTcNormLimit)) atomicExch(err, 1);  // see kTcNormLimit
 }
 
 struct TcArgs {
@@ -258,15 +270,18 @@ __device__ __forceinline__ uint32_t core_offset(int row, int kb, int KB) {
 // [-2q, 1] (queries) or [r, |r|^2] (references).
 template <int MODE>
 __global__ void k_tc5_pack(const float* __restrict__ x, int rows, int rows_pad, int d, int KP, int tile_rows,
-                           int is_query, unsigned char* __restrict__ hi, unsigned char* __restrict__ lo) {
+                           int is_query, unsigned char* __restrict__ hi, unsigned char* __restrict__ lo,
+                           int* __restrict__ err) {
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= rows_pad) return;
     constexpr int ESZ = MODE == TK_BRUTE_TF32 ? 4 : 2;
     const int KB = KP * ESZ;
     const bool real = r < rows;
     float nrm = 0.f;
-    if (real && !is_query)
+    if (real && !is_query) {
         for (int c = 0; c < d; ++c) nrm = fmaf(x[(long long)r * d + c], x[(long long)r * d + c], nrm);
+        if (!(nrm < kTcNormLimit)) atomicExch(err, 1);  // see kTcNormLimit
+    }
     const long long tile_base = (long long)(r / tile_rows) * tile_rows * KB;
     const int rr = r % tile_rows;
     for (int c = 0; c < KP; ++c) {
@@ -746,10 +761,11 @@ __global__ void __launch_bounds__(256) k_tc_rerank(const RerankArgs a) {
         double tau = INFINITY;
         for (int s = 0; s < a.nsplit; ++s) tau = fmin(tau, (double)a.tau[(long long)qi * a.nsplit + s]);
         bool ok = !(a.err && *a.err);
+        double qq = 0.0;
+        for (int c = 0; c < a.d; ++c) qq += (double)qrow[c] * (double)qrow[c];
+        ok = ok && qq < double(kTcNormLimit);  // see kTcNormLimit (false for NaN / inf coordinates)
         if (ok && !isinf(tau)) {
             const double D = (double)worst.dist();
-            double qq = 0.0;
-            for (int c = 0; c < a.d; ++c) qq += (double)qrow[c] * (double)qrow[c];
             const double u = 1.0 / 16777216.0;                  // 2^-24
             const double m = (a.d + 4) * u;                      // rounding of the exact FP32 distance
             const double Dp = D / (1.0 - m);                     // real |q-r|^2 of any r with dist(r) <= D
