@@ -321,3 +321,49 @@ def test_infinite_and_huge_reference_points(dims, oracle):
         d, i = gpu_query(ref, q, 5, levels=7, **opts)
         np.testing.assert_array_equal(d, bd, err_msg=str(opts))
         np.testing.assert_array_equal(i, bi, err_msg=str(opts))
+
+
+@pytest.mark.parametrize("n", [1, 2, 3])
+def test_trees_of_one_to_three_points(n, oracle):
+    rng = np.random.default_rng(90 + n)
+    ref = rng.standard_normal((n, 3)).astype(np.float32)
+    q = rng.standard_normal((50, 3)).astype(np.float32)
+    for k in range(1, n + 1):
+        bd, bi = oracle.brute(ref, q, k)
+        for opts in (dict(), dict(threads_per_query=32), dict(traversal=2)):
+            d, i = gpu_query(ref, q, k, **opts)
+            np.testing.assert_array_equal(d, bd, err_msg=str(opts))
+            np.testing.assert_array_equal(i, bi, err_msg=str(opts))
+
+
+def test_concurrent_queries_on_one_tree():
+    """Four threads, each on its own stream, query one tree at the same time
+    (the tree is read-only; each call has its own workspace)."""
+    import threading
+    rng = np.random.default_rng(95)
+    tree = tk().build_kd_tree(torch.from_numpy(rng.random((200000, 3), dtype=np.float32)).to(cuda))
+    qs = [torch.from_numpy(rng.random((150000 + 11 * t, 3), dtype=np.float32)).to(cuda) for t in range(4)]
+    ks = [1, 8, 16, 40]
+    want = [tree.query(q, nr_nns_searches=k) for q, k in zip(qs, ks)]
+    torch.cuda.synchronize()
+    got, errors = [None] * 4, []
+
+    def work(t):
+        try:
+            torch.cuda.set_device(0)
+            s = torch.cuda.Stream()
+            with torch.cuda.stream(s):
+                for _ in range(3):
+                    got[t] = tree.query(qs[t], nr_nns_searches=ks[t])
+            s.synchronize()
+        except Exception as e:  # reported below
+            errors.append(e)
+
+    threads = [threading.Thread(target=work, args=(t,)) for t in range(4)]
+    for th in threads:
+        th.start()
+    for th in threads:
+        th.join()
+    assert not errors, errors
+    for (wd, wi), (d, i) in zip(want, got):
+        assert torch.equal(d, wd) and torch.equal(i, wi)
