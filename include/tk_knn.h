@@ -3,8 +3,11 @@
  *
  * Drop-in boundary for torch_kdtree's query path.  Every entry point takes
  * plain pointers and sizes, returns a tk_status, never exits the process and
- * never allocates device memory on a query path: scratch memory is passed in
- * by the caller (sizes from the *_workspace_size functions).  Device work is
+ * never allocates device memory on a query path (tk_tree_query_host, whose
+ * device staging is kept per tree, excepted): scratch memory is passed in by
+ * the caller (sizes from the *_workspace_size functions; 256-byte aligned, as
+ * cudaMalloc returns it -- a misaligned workspace fails with TK_EINVAL before
+ * any device work).  Device work is
  * enqueued on the caller's CUDA stream (a cudaStream_t passed as void*; NULL
  * = the legacy default stream, which is what the reference used) and is
  * asynchronous, like the reference's KDTreeKNNGPUSearch.

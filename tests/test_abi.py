@@ -132,6 +132,26 @@ def test_error_paths_without_gpu():
     LIB.tk_tree_destroy(h)
 
 
+def test_misaligned_workspace_is_refused_before_device_work():
+    """Workspaces are carved into 256-byte aligned sub-buffers (some read by bulk
+    copies): a misaligned one fails with TK_EINVAL before anything touches a GPU."""
+    from torch_kdtree_gb300._lib import LIB, TK_EINVAL
+    ref = np.zeros((100, 3), np.float32)
+    q = np.zeros((10, 3), np.float32)
+    d = np.empty((10, 2), np.float32)
+    i = np.empty((10, 2), np.int32)
+    g = np.zeros((10, 2), np.float32)
+    ws = np.zeros(1 << 20, np.uint8)
+    aligned = (ws.ctypes.data + 255) // 256 * 256
+    for off in (4, 16, 128):
+        st = LIB.tk_nn_distance(ref.ctypes.data, 100, q.ctypes.data, 10, 3, 2, 0, 0, d.ctypes.data, i.ctypes.data,
+                                aligned + off, 1 << 19, None)
+        assert st == TK_EINVAL and "256-byte aligned" in LIB.tk_last_error().decode()
+        st = LIB.tk_knn_backward(q.ctypes.data, ref.ctypes.data, i.ctypes.data, g.ctypes.data, 10, 100, 2, 3, 0,
+                                 None, ref.ctypes.data, aligned + off, 1 << 19, None)
+        assert st == TK_EINVAL and "256-byte aligned" in LIB.tk_last_error().decode()
+
+
 def test_default_levels_matches_reference_heuristic():
     from torch_kdtree_gb300 import default_levels
     for n, L in [(5, 1), (30, 1), (1000, 6), (100_000, 13), (4_194_304, 13), (16, 1), (128, 4)]:

@@ -182,6 +182,7 @@ int tk_knn_backward(const void* q, const void* ref, const int32_t* idx, const vo
     if (!q || !ref || !idx || !grad_dists) return fail(TK_EINVAL, "null input pointer");
     if (grad_ref && (!workspace || workspace_bytes < bw_layout(nq, k, n).total))
         return fail(TK_EWORKSPACE, "workspace too small");
+    if (ws_misaligned(workspace)) return fail(TK_EINVAL, "workspace must be 256-byte aligned");
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     char* ws = static_cast<char*>(workspace);
     const int nq32 = int(nq), n32 = int(n);

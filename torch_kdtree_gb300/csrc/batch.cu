@@ -332,6 +332,7 @@ int tk_batch_query(const tk_batch* b, const void* q, void* dists, int32_t* idx, 
     if (b->total_q == 0) return TK_OK;
     if (!q || !dists || !idx) return fail(TK_EINVAL, "null pointer");
     if (!workspace || workspace_bytes < batch_ws(b).total) return fail(TK_EWORKSPACE, "workspace too small");
+    if (ws_misaligned(workspace)) return fail(TK_EINVAL, "workspace must be 256-byte aligned");
     int G = threads_per_query;
     if (G <= 0) G = b->max_k <= 16 ? 1 : 8;
     if (G != 1 && G != 8) return fail(TK_EINVAL, "batched queries run 1 or 8 lanes per query");

@@ -209,6 +209,7 @@ int tk_nn_distance(const void* ref, int64_t n, const void* q, int64_t nq, int di
     int rc = check_common(ref, n, q, nq, dims, k, dtype, dists, idx);
     if (rc != TK_OK) return rc;
     if (nq == 0) return TK_OK;
+    if (ws_misaligned(workspace)) return fail(TK_EINVAL, "workspace must be 256-byte aligned");
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     if (mode == TK_BRUTE_EXACT) {
         if (dtype == TK_F32)

@@ -687,6 +687,7 @@ int tk_tree_query(const tk_tree* t, const void* q, int64_t nq, int k, void* dist
     const size_t need = ws_layout(t->levels, nq).total;
     if (!workspace || workspace_bytes < need)
         return fail(TK_EWORKSPACE, "workspace too small: need " + std::to_string(need) + " bytes");
+    if (ws_misaligned(workspace)) return fail(TK_EINVAL, "workspace must be 256-byte aligned");
     tk_query_opts o{0, -1, -1, 0, 0, nullptr, nullptr, -1, 0};
     if (opts) o = *opts;
     DeviceGuard g(t->device);

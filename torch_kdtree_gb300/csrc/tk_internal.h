@@ -22,6 +22,11 @@ inline int record_width(int dims) { return dims <= 3 ? 3 : (dims <= 4 ? 4 : 8); 
 
 // Sets the thread-local error text and returns the status.
 int fail(int status, const std::string& msg);
+
+// Caller workspaces are carved into 256-byte aligned sub-buffers (some are
+// read by bulk copies, which need 16-byte alignment), so the caller's pointer
+// must be 256-byte aligned, as cudaMalloc's are.
+inline bool ws_misaligned(const void* p) { return p && (reinterpret_cast<uintptr_t>(p) & 255) != 0; }
 void clear_error();
 
 // Host copy of a tree in the reference's layout (src/kdtree.hpp:126-217) plus
