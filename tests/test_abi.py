@@ -39,6 +39,50 @@ def test_library_exports_every_declared_symbol():
     assert not [n for n in declared_functions() if n not in _lib.SIGNATURES]
 
 
+C_PROGRAM = r"""
+#include <stdio.h>
+#include "tk_knn.h"
+int main(void) {
+    float pts[8 * 3];
+    int32_t perm[8];
+    float dists[2], q[3] = {0.f, 0.f, 0.f};
+    int32_t idx[2];
+    tk_tree* tree = NULL;
+    tk_tree_info info;
+    for (int i = 0; i < 8 * 3; ++i) pts[i] = (float)((i * 7) % 11);
+    if (tk_tree_create(pts, 8, 3, TK_F32, 2, -1, 1, &tree) != TK_OK) return 1;  /* host-only tree */
+    if (tk_tree_get_info(tree, &info) != TK_OK || info.n_points != 8 || info.dims != 3) return 2;
+    if (tk_tree_get_perm(tree, perm) != TK_OK) return 3;
+    /* queries need a device image: refused, with a message, never computed on the CPU */
+    if (tk_tree_query_host(tree, q, 1, 2, dists, idx, NULL, TK_HOST_AUTO, NULL) != TK_EINVAL) return 4;
+    if (tk_last_error()[0] == 0) return 5;
+    tk_tree_destroy(tree);
+    printf("ok %d\n", tk_version());
+    return 0;
+}
+"""
+
+
+def test_header_is_c99_and_links_from_c(tmp_path):
+    """The boundary is plain C: the header compiles as strict C99 and a C
+    program links against libtkknn.so and runs (host-only calls, no GPU)."""
+    import shutil
+    import subprocess
+    from torch_kdtree_gb300 import _lib
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    src = tmp_path / "use_tk.c"
+    src.write_text(C_PROGRAM)
+    exe = tmp_path / "use_tk"
+    libdir = os.path.dirname(_lib.LIB_PATH)
+    subprocess.run([cc, "-std=c99", "-Wall", "-Wextra", "-Werror", "-I", os.path.join(ROOT, "include"), str(src),
+                    "-o", str(exe), "-L", libdir, "-ltkknn", "-Wl,-rpath," + libdir], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert out.returncode == 0, (out.returncode, out.stdout, out.stderr)
+    assert out.stdout.startswith("ok ")
+
+
 def host_tree(points, levels):
     from torch_kdtree_gb300._lib import LIB, TkError, check  # noqa: F401
     h = ctypes.c_void_p()
