@@ -104,18 +104,24 @@ bool gr_available(int dtype, int dims, int G, int R) {
     return true;
 }
 
-// Lanes per query when the caller leaves it open (measured on 1M-query
-// workloads): one lane per query up to ~192 points per leaf and k <= 16 (its
-// list fits one lane's registers); 32 lanes for larger leaves or k > 16,
+// Lanes per query when the caller leaves it to the library (measured on the
+// large workloads): one lane per query up to ~192 points per leaf and k <= 16
+// (its list fits one lane's registers); 32 lanes for larger leaves or k > 16,
 // which spread both the leaf scan and the list (k = 100: 21 ms on 32 lanes,
-// 35 ms on 8).  For small query counts, enough lanes to give every SM about
-// 1024 threads (10,000 queries on one lane each fill only 40 of 152 SMs; 16
-// lanes each ran 1.6x faster).
+// 35 ms on 8).  Calls with fewer queries than half a wave (SMs x 512) spread
+// each query over 4, 8, 16 or 32 lanes until queries x lanes fill a wave of
+// SMs x 1024 threads: 10,000 queries on one lane each fill 40 of 152 SMs and
+// ran 1.6x slower than on 16 lanes; at 32,768 (65,536) queries 8 (4) lanes
+// beat one by 25% (6%), while at 131,072 one lane beat two by 20%.  Two-lane
+// groups were the slowest shape in every measurement and are skipped.
 int auto_lanes(const tk_tree* t, int64_t nq, int k) {
     const double avg_leaf = double(t->n) / double(int64_t(1) << t->levels);
     int g = (k > 16 || avg_leaf > 192) ? 32 : 1;
-    const int64_t target = int64_t(sm_count(t->device)) * 1024;
-    while (g < 32 && nq * g < target) g <<= 1;
+    const int64_t wave = int64_t(sm_count(t->device)) * 1024;  // resident threads
+    if (g == 1 && 2 * nq < wave) {
+        g = 4;
+        while (g < 32 && nq * g < wave) g <<= 1;
+    }
     return g;
 }
 
@@ -135,7 +141,14 @@ int prepare_order(const tk_tree* t, int nq, const tk_query_opts& o, char* ws, cu
     const WsLayout w = ws_layout(L, nq);
     *counter = reinterpret_cast<int*>(ws + w.counter);
     *order = nullptr;
-    const bool bin = o.bin_queries == 1 || (o.bin_queries < 0 && nq >= 1024 && L >= 2);
+    // Automatic binning from one wave of queries (SMs x 1024) on: below that
+    // each thread takes about one query, the cell order gains little leaf
+    // sharing, and grouping a region's expensive queries into the same warps
+    // lengthens the slowest warp, which then sets the launch time (131,072
+    // queries: 1.33 ms binned vs 1.17 ms in input order; 1,048,576: 3.53 vs
+    // 5.84 ms on the cube-and-sphere workload).
+    const bool bin = o.bin_queries == 1 ||
+                     (o.bin_queries < 0 && L >= 2 && int64_t(nq) >= int64_t(sm_count(t->device)) * 1024);
     cudaError_t e;
     if (bin) {
         const int B = bin_levels(L, nq);
