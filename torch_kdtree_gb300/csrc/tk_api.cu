@@ -113,10 +113,14 @@ bool gr_available(int dtype, int dims, int G, int R) {
 // SMs x 1024 threads: 10,000 queries on one lane each fill 40 of 152 SMs and
 // ran 1.6x slower than on 16 lanes; at 32,768 (65,536) queries 8 (4) lanes
 // beat one by 25% (6%), while at 131,072 one lane beat two by 20%.  Two-lane
-// groups were the slowest shape in every measurement and are skipped.
+// groups were the slowest shape in every measurement and are skipped.  Trees
+// of 4-8 dimensions (1M refs x 262k queries N(0,1), depth 12-13): one lane
+// only for k = 1 up to 6 dimensions (d=4: 0.40 vs 0.70 ms), 32 otherwise
+// (d=8, k=16: 21.4 vs 38.3 ms; d=8, k=1: 8.5 vs 9.1 ms).
 int auto_lanes(const tk_tree* t, int64_t nq, int k) {
     const double avg_leaf = double(t->n) / double(int64_t(1) << t->levels);
     int g = (k > 16 || avg_leaf > 192) ? 32 : 1;
+    if (t->dims > 3) g = (k == 1 && t->dims <= 6) ? 1 : 32;
     const int64_t wave = int64_t(sm_count(t->device)) * 1024;  // resident threads
     if (g == 1 && 2 * nq < wave) {
         g = 4;
