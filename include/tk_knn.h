@@ -228,7 +228,7 @@ size_t tk_nn_distance_workspace_size(int64_t n, int64_t nq, int dims, int k, int
 
 /* Exhaustive exact k nearest neighbours (the nn_distance op).
  * ref: device [n, dims]; q: device [nq, dims]; dists [nq, k] squared
- * distances, idx int32 [nq, k]; 1 <= dims <= 128 (float64: dims <= 4),
+ * distances, idx int32 [nq, k]; 1 <= dims <= 128 (float32 or float64),
  * 1 <= k <= min(n, 128).  Every mode returns the same answer as the KD-tree
  * query: ordered by (distance computed as the reference does, index).
  * Replaces NmDistanceKernelLauncherDynamic (src/nndistance_g.cu:191-220),

@@ -28,15 +28,29 @@ def test_exact_mode_matches_oracle(d, k, oracle):
     np.testing.assert_array_equal(ii.cpu().numpy(), bi)
 
 
-@pytest.mark.parametrize("d", [1, 2, 3])
+@pytest.mark.parametrize("d", [1, 2, 3, 5, 8, 17, 40, 128])
 def test_float64(d, oracle):
+    """FP64 stays FP64 end to end, at any dimension."""
     rng = np.random.default_rng(40 + d)
     ref = rng.standard_normal((5000, d))
     q = rng.standard_normal((500, d))
-    dd, ii = tk().nn_distance(torch.from_numpy(ref).to(cuda), torch.from_numpy(q).to(cuda), 7)
-    bd, bi = oracle.brute(ref, q, 7)
-    np.testing.assert_array_equal(dd.cpu().numpy(), bd)
-    np.testing.assert_array_equal(ii.cpu().numpy(), bi)
+    for k in (1, 7, 40):
+        dd, ii = tk().nn_distance(torch.from_numpy(ref).to(cuda), torch.from_numpy(q).to(cuda), k)
+        assert dd.dtype == torch.float64
+        bd, bi = oracle.brute(ref, q, k)
+        np.testing.assert_array_equal(dd.cpu().numpy(), bd)
+        np.testing.assert_array_equal(ii.cpu().numpy(), bi)
+    if d in (5, 40):  # gradients in float64 as well
+        r = torch.from_numpy(ref).to(cuda).requires_grad_(True)
+        qq = torch.from_numpy(q).to(cuda).requires_grad_(True)
+        dd, ii = tk().nn_distance(r, qq, 7)
+        w = torch.rand_like(dd)
+        (dd * w).sum().backward()
+        r2 = r.detach().clone().requires_grad_(True)
+        q2 = qq.detach().clone().requires_grad_(True)
+        ((q2[:, None] - r2[ii.long()]) ** 2).sum(-1).mul(w).sum().backward()
+        assert torch.allclose(qq.grad, q2.grad, rtol=1e-12, atol=1e-12)
+        assert torch.allclose(r.grad, r2.grad, rtol=1e-12, atol=1e-12)
 
 
 def test_brute_equals_kdtree():

@@ -44,10 +44,6 @@ int padded_dims(int d) {
     return 128;
 }
 
-struct BrutePlan {
-    int DP, G, R, nsplit, qtiles;
-};
-
 BrutePlan plan_brute(int64_t n, int64_t nq, int d, int k, bool f32) {
     BrutePlan p;
     p.DP = padded_dims(d);
@@ -73,27 +69,6 @@ template <typename T>
 size_t brute_ws_bytes(const BrutePlan& p, int64_t nq, int k) {
     if (p.nsplit <= 1) return 256;
     return align256(sizeof(Key<T>) * size_t(nq) * p.nsplit * k);
-}
-
-template <typename T, int DP>
-int launch_dp(const BruteArgs<T>& a, const BrutePlan& p, cudaStream_t s) {
-    dim3 grid(p.qtiles, p.nsplit);
-    bool done = false;
-#define TK_BR(g, r)                                                          \
-    if (!done && p.G == g && p.R == r) {                                     \
-        k_brute<T, DP, g, r><<<grid, 256, 0, s>>>(a);                        \
-        if (p.nsplit > 1) k_brute_merge<T, g, r><<<p.qtiles, 256, 0, s>>>(a); \
-        done = true;                                                         \
-    }
-    TK_BR(1, 1) TK_BR(1, 4) TK_BR(1, 16) TK_BR(2, 16) TK_BR(4, 16) TK_BR(8, 16)
-    if constexpr (sizeof(T) == 4 && DP % 4 == 0 && DP <= 32) {
-        TK_BR(1, 32)
-    }
-#undef TK_BR
-    if (!done) return fail(TK_EUNSUPPORTED, "no brute-force kernel for this k");
-    const cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return fail(TK_ECUDA, std::string("brute-force launch: ") + cudaGetErrorString(e));
-    return TK_OK;
 }
 
 template <typename T>
@@ -129,8 +104,10 @@ int run_brute(const T* ref, int64_t n, const T* q, int64_t nq, int d, int k, T* 
             case 128: return launch_dp<T, 128>(a, p, s);
             default: break;
         }
+    } else {
+        return launch_brute_f64_wide(a, p, s);  // brute_f64.cu: d = 5 .. 128
     }
-    return fail(TK_EUNSUPPORTED, "float64 brute force supports d <= 4");
+    return fail(TK_EUNSUPPORTED, "no brute-force kernel for this dimension");
 }
 
 int check_common(const void* ref, int64_t n, const void* q, int64_t nq, int d, int k, int dtype, const void* dists,

@@ -39,9 +39,11 @@ struct BruteArgs {
     const int* qcount = nullptr;
 };
 
-template <int DP>
+// Reference rows per shared-memory tile: 32 KiB of coordinates, 32 to 256 rows.
+template <typename T, int DP>
 struct BruteTile {
-    static constexpr int kRefs = (8192 / DP) > 256 ? 256 : ((8192 / DP) < 32 ? 32 : (8192 / DP));
+    static constexpr int kElems = 32768 / int(sizeof(T));
+    static constexpr int kRefs = (kElems / DP) > 256 ? 256 : ((kElems / DP) < 32 ? 32 : (kElems / DP));
 };
 
 template <typename T, int DP>
@@ -58,7 +60,7 @@ __device__ __forceinline__ T sqdist_padded(const T (&q)[DP], const T* r) {
 
 template <typename T, int DP, int G, int R>
 __global__ void __launch_bounds__(256) k_brute(const BruteArgs<T> a) {
-    constexpr int TR = BruteTile<DP>::kRefs;
+    constexpr int TR = BruteTile<T, DP>::kRefs;
     __shared__ __align__(16) T tile[TR * DP];
     const int lane = threadIdx.x & 31;
     const int gl = lane & (G - 1);
@@ -214,5 +216,34 @@ __global__ void __launch_bounds__(256) k_brute_merge(const BruteArgs<T> a) {
 size_t brute_fallback_workspace_bytes(int64_t n, int64_t nq, int d, int k);
 int brute_fallback(const float* ref, int64_t n, const float* q, int64_t nq, int d, int k, float* dists,
                    int32_t* idx, const int* qlist, const int* qcount, void* ws, size_t ws_bytes, cudaStream_t s);
+
+// Launch shape of an exhaustive search (brute.cu: plan_brute).
+struct BrutePlan {
+    int DP, G, R, nsplit, qtiles;
+};
+
+template <typename T, int DP>
+int launch_dp(const BruteArgs<T>& a, const BrutePlan& p, cudaStream_t s) {
+    dim3 grid(p.qtiles, p.nsplit);
+    bool done = false;
+#define TK_BR(g, r)                                                          \
+    if (!done && p.G == g && p.R == r) {                                     \
+        k_brute<T, DP, g, r><<<grid, 256, 0, s>>>(a);                        \
+        if (p.nsplit > 1) k_brute_merge<T, g, r><<<p.qtiles, 256, 0, s>>>(a); \
+        done = true;                                                         \
+    }
+    TK_BR(1, 1) TK_BR(1, 4) TK_BR(1, 16) TK_BR(2, 16) TK_BR(4, 16) TK_BR(8, 16)
+    if constexpr (sizeof(T) == 4 && DP % 4 == 0 && DP <= 32) {
+        TK_BR(1, 32)
+    }
+#undef TK_BR
+    if (!done) return fail(TK_EUNSUPPORTED, "no brute-force kernel for this k");
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(TK_ECUDA, std::string("brute-force launch: ") + cudaGetErrorString(e));
+    return TK_OK;
+}
+
+// float64 searches of 5 to 128 dimensions (brute_f64.cu, a unit of its own).
+int launch_brute_f64_wide(const BruteArgs<double>& a, const BrutePlan& p, cudaStream_t s);
 
 }  // namespace tk

@@ -380,7 +380,7 @@ def nn_distance(points_ref: torch.Tensor, points_query: torch.Tensor, nr_nns_sea
     by :func:`torch_kdtree_gb300.autotune.autotune_brute` and cached).
     Differentiable in both point sets.  The reference shipped this search as
     an unbound CUDA launcher (src/nndistance_g.cu:191-220) for d = 3 only;
-    here any 1 <= d <= 128 (float64: d <= 4)."""
+    here any 1 <= d <= 128, float32 or float64."""
     if mode not in _BRUTE_MODES and mode != "auto":
         raise ValueError(f"mode must be one of {sorted(_BRUTE_MODES) + ['auto']}")
     if points_ref.device.type != "cuda":
