@@ -7,11 +7,20 @@
 // Here:
 //   grad_q[i]   = sum_j 2 g[i, j] (q[i] - ref[idx[i, j]])       (a gather, j ascending)
 //   grad_ref[m] = sum_{(i,j): idx[i,j] = m} 2 g[i, j] (ref[m] - q[i])
-// grad_ref is a segmented reduction: the (idx, pair) list is sorted by a
-// stable radix sort, so each reference point sees its pairs in ascending
-// pair order and one thread sums them in that fixed order -- bitwise
-// reproducible, no float atomics.  Differences are recomputed from the saved
-// indices; nothing of size [Q, k, d] is stored.
+// grad_ref is a segmented reduction over the indices, bitwise reproducible and
+// without float atomics, in one of two forms:
+//  * float32, d <= 3: segments are built by counting (integer atomics), a
+//    scan and an atomic fill, so the order inside a segment is arbitrary; the
+//    segment's sum is made order-independent instead.  One pass finds the
+//    largest exponent of its terms per coordinate, a second adds every FP32
+//    term exactly as a 64-bit fixed-point integer scaled to that exponent,
+//    and the total is rounded once -- the same bits whatever the order, and
+//    closer to the exact sum than a sequential FP32 sum;
+//  * otherwise: the (idx, pair) list is sorted by a stable radix sort, so
+//    each reference point sees its pairs in ascending pair order and one
+//    thread sums them in that fixed order.
+// Differences are recomputed from the saved indices; nothing of size
+// [Q, k, d] is stored.
 #include <algorithm>
 #include <string>
 
@@ -98,8 +107,116 @@ __global__ void k_grad_ref(const T* __restrict__ q, const T* __restrict__ ref, c
         if (c < d) grad_ref[(long long)m * d + c] = acc[c];
 }
 
+// Segments by counting (float32, d <= 3): counts of every key, then their
+// exclusive scan (n + 1 entries: starts, and the total at n).
+__global__ void k_count_keys(const int32_t* __restrict__ idx, long long npairs, int n, int* __restrict__ cnt) {
+    const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= npairs) return;
+    const int m = idx[p];
+    if (m >= 0 && m < n) atomicAdd(cnt + m, 1);
+}
+
+// Every valid pair into its key's segment, in arbitrary order.
+__global__ void k_fill_segments(const int32_t* __restrict__ idx, long long npairs, int n,
+                                const int* __restrict__ starts, int* __restrict__ cursor, uint32_t* __restrict__ list) {
+    const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= npairs) return;
+    const int m = idx[p];
+    if (m < 0 || m >= n) return;
+    list[starts[m] + atomicAdd(cursor + m, 1)] = uint32_t(p);
+}
+
+// Exponent field of a float (0 for zeros and subnormals, 255 for inf / NaN).
+__device__ __forceinline__ int exp_field(float t) { return int((__float_as_uint(t) >> 23) & 0xFFu); }
+
+// 2^e as a double, e in [-1022, 1023].
+__device__ __forceinline__ double pow2(int e) { return __longlong_as_double((long long)(1023 + e) << 52); }
+
+// t * 2^sh rounded to the nearest integer (halves away from zero), in integer
+// arithmetic: a finite float is mant * 2^(max(e, 1) - 150) with its 24-bit
+// significand mant.  The caller guarantees |t * 2^sh| < 2^61.
+__device__ __forceinline__ long long to_fixed(float t, int sh) {
+    const uint32_t b = __float_as_uint(t);
+    const int e = int((b >> 23) & 0xFFu);
+    const long long mant = (long long)((b & 0x7FFFFFu) | (e ? 0x800000u : 0u));
+    const int amt = (e ? e : 1) - 150 + sh;
+    long long v;
+    if (amt >= 0)
+        v = mant << amt;
+    else if (amt > -25)
+        v = (mant + (1ll << (-amt - 1))) >> (-amt);
+    else
+        v = 0;  // below half a unit
+    return (b >> 31) ? -v : v;
+}
+
+// One thread per reference point: the order-independent sum of its segment
+// (see the top of this file).  A term t has |t| < 2^(E - 126) for the largest
+// exponent field E of its coordinate; scaled by 2^(187 - L - E), with s <
+// 2^L terms in the segment, each scaled term is below 2^(61 - L) and the sum
+// below 2^61, so the int64 accumulator cannot overflow.  Each scaled term is
+// rounded to an integer once (to_fixed), by a rule that does not depend on
+// the order.
+template <int D>
+__global__ void k_grad_ref_fixed(const float* __restrict__ q, const float* __restrict__ ref, const float* __restrict__ g,
+                                 const uint32_t* __restrict__ list, const int* __restrict__ starts, int n, int k,
+                                 float* __restrict__ grad_ref) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= n) return;
+    float rm[D];
+#pragma unroll
+    for (int c = 0; c < D; ++c) rm[c] = ref[(long long)m * D + c];
+    const int s0 = starts[m], s1 = starts[m + 1];
+    int emax[D];
+#pragma unroll
+    for (int c = 0; c < D; ++c) emax[c] = 0;
+    bool finite = true;
+    for (int j = s0; j < s1; ++j) {
+        const uint32_t p = list[j];
+        const long long i = (long long)(p / uint32_t(k));
+        const float w = 2.f * g[p];
+#pragma unroll
+        for (int c = 0; c < D; ++c) {
+            const int e = exp_field(__fmul_rn(w, __fsub_rn(rm[c], q[i * D + c])));
+            finite = finite && e != 255;
+            emax[c] = max(emax[c], e);
+        }
+    }
+    float out[D];
+    if (!finite) {
+        // an infinite or NaN term: the sum is +-inf or NaN in any order
+#pragma unroll
+        for (int c = 0; c < D; ++c) out[c] = 0.f;
+        for (int j = s0; j < s1; ++j) {
+            const uint32_t p = list[j];
+            const long long i = (long long)(p / uint32_t(k));
+            const float w = 2.f * g[p];
+#pragma unroll
+            for (int c = 0; c < D; ++c) out[c] += __fmul_rn(w, __fsub_rn(rm[c], q[i * D + c]));
+        }
+    } else {
+        const int L = 32 - __clz(s1 - s0);  // s1 - s0 < 2^L
+        long long acc[D];
+#pragma unroll
+        for (int c = 0; c < D; ++c) acc[c] = 0;
+        for (int j = s0; j < s1; ++j) {
+            const uint32_t p = list[j];
+            const long long i = (long long)(p / uint32_t(k));
+            const float w = 2.f * g[p];
+#pragma unroll
+            for (int c = 0; c < D; ++c)
+                acc[c] += to_fixed(__fmul_rn(w, __fsub_rn(rm[c], q[i * D + c])), 187 - L - emax[c]);
+        }
+#pragma unroll
+        for (int c = 0; c < D; ++c) out[c] = float(double(acc[c]) * pow2(emax[c] + L - 187));
+    }
+#pragma unroll
+    for (int c = 0; c < D; ++c) grad_ref[(long long)m * D + c] = out[c];
+}
+
 struct BwLayout {
-    size_t keys = 0, sorted_keys = 0, sorted_vals = 0, seg_end = 0, seg_start = 0, sort_ws = 0, total = 0;
+    size_t keys = 0, sorted_keys = 0, sorted_vals = 0, seg_end = 0, seg_start = 0, sort_ws = 0, scan_ws = 0,
+           total = 0;
 };
 
 BwLayout bw_layout(int64_t nq, int k, int64_t n) {
@@ -112,12 +229,14 @@ BwLayout bw_layout(int64_t nq, int k, int64_t n) {
     o += align256(4 * size_t(np));
     w.sorted_vals = o;
     o += align256(4 * size_t(np));
-    w.seg_end = o;
-    o += align256(4 * size_t(std::max<int64_t>(n, 1)));
+    w.seg_end = o;  // also the n + 1 counts / starts of the counting path
+    o += align256(4 * size_t(std::max<int64_t>(n, 1) + 1));
     w.seg_start = o;
     o += align256(4 * size_t(std::max<int64_t>(n, 1)));
     w.sort_ws = o;
     o += sort_workspace_bytes(np);
+    w.scan_ws = o;
+    o += scan_workspace_bytes(std::max<int64_t>(n, 1) + 1);
     w.total = o;
     return w;
 }
@@ -133,7 +252,25 @@ int run_backward(const T* q, const T* ref, const int32_t* idx, const T* g, int n
                  T* grad_ref, char* ws, cudaStream_t s) {
     const int bs = D > 32 ? 64 : 256;
     if (grad_q) k_grad_q<T, D><<<(nq + bs - 1) / bs, bs, 0, s>>>(q, ref, idx, g, nq, n, k, d, grad_q);
-    if (grad_ref) {
+    if (grad_ref && sizeof(T) == 4 && D <= 3) {
+        const BwLayout w = bw_layout(nq, k, n);
+        const long long np = (long long)nq * k;
+        int* starts = reinterpret_cast<int*>(ws + w.seg_end);      // n + 1
+        int* cursor = reinterpret_cast<int*>(ws + w.seg_start);    // n
+        uint32_t* list = reinterpret_cast<uint32_t*>(ws + w.sorted_vals);
+        cudaError_t e = cudaMemsetAsync(starts, 0, sizeof(int) * (size_t(n) + 1), s);
+        if (e == cudaSuccess) e = cudaMemsetAsync(cursor, 0, sizeof(int) * size_t(n), s);
+        if (e != cudaSuccess) return fail(TK_ECUDA, std::string("memset: ") + cudaGetErrorString(e));
+        if (np > 0) k_count_keys<<<unsigned((np + 255) / 256), 256, 0, s>>>(idx, np, n, starts);
+        e = exclusive_scan(starts, int64_t(n) + 1, ws + w.scan_ws, s);
+        if (e != cudaSuccess) return fail(TK_ECUDA, std::string("backward scan: ") + cudaGetErrorString(e));
+        if (np > 0) k_fill_segments<<<unsigned((np + 255) / 256), 256, 0, s>>>(idx, np, n, starts, cursor, list);
+        if constexpr (sizeof(T) == 4 && D <= 3)
+            k_grad_ref_fixed<D><<<(n + 255) / 256, 256, 0, s>>>(reinterpret_cast<const float*>(q),
+                                                                 reinterpret_cast<const float*>(ref),
+                                                                 reinterpret_cast<const float*>(g), list, starts, n, k,
+                                                                 reinterpret_cast<float*>(grad_ref));
+    } else if (grad_ref) {
         const BwLayout w = bw_layout(nq, k, n);
         const long long np = (long long)nq * k;
         uint32_t* keys = reinterpret_cast<uint32_t*>(ws + w.keys);
