@@ -26,7 +26,7 @@ def torch_indexed_grads(q, ref, inds, w):
 
 
 @pytest.mark.parametrize("dtype,tol", [(torch.float32, 1e-5), (torch.float64, 1e-12)])
-@pytest.mark.parametrize("d", [1, 2, 3])
+@pytest.mark.parametrize("d", [1, 2, 3, 5, 8])
 def test_matches_torch_indexed_gradient(dtype, tol, d):
     g = torch.Generator(device="cpu").manual_seed(7)
     ref = torch.randn(20000, d, generator=g, dtype=dtype).to(cuda).requires_grad_(True)
@@ -101,3 +101,33 @@ def test_finite_differences_fp64():
             fd = ((loss(q64, r64 + e) - loss(q64, r64 - e)) / (2 * h)).item()
             an = ref.grad[m, c].item()
             assert abs(an - fd) <= 1e-3 * max(abs(fd), 1e-3), (m, c, an, fd)
+
+
+@pytest.mark.parametrize("d", [3, 6, 16])
+def test_hub_segments_are_deterministic_and_accurate(d):
+    """Every query shares the same few neighbours (segments of 100,000+ pairs):
+    the order-independent fixed-point sums (d <= 8) and the sorted segments
+    (d = 16) give the same bits on every run and match an FP64 sum."""
+    g = torch.Generator(device="cpu").manual_seed(9)
+    ref = torch.randn(5000, d, generator=g)
+    ref[:8] = 40.0 + torch.randn(8, d, generator=g) * 1e-3  # a far-away cluster of 8 points
+    q = 40.0 + torch.randn(120000, d, generator=g) * 1e-2    # all queries next to it
+    ref, q = ref.to(cuda), q.to(cuda)
+    w = torch.rand(120000, 8, generator=g).to(cuda)
+    outs = []
+    for _ in range(3):
+        r = ref.clone().requires_grad_(True)
+        qq = q.clone().requires_grad_(True)
+        dists, inds = tk().nn_distance(r, qq, 8)
+        (0.5 * (dists * w).sum()).backward()
+        outs.append(r.grad.clone())
+    assert (inds.long() < 8).all()
+    for gr in outs[1:]:
+        assert torch.equal(gr, outs[0])
+    # FP64 sum of the same terms
+    r64, q64, w64 = ref.double(), q.double(), w.double()
+    terms = (w64[..., None] * (r64[inds.long()] - q64[:, None]))  # 2 * 0.5 * w * (r - q)
+    exact = torch.zeros_like(r64).index_add_(0, inds.long().reshape(-1), terms.reshape(-1, d))
+    err = (outs[0].double() - exact).abs().max().item()
+    # fixed-point sums: one rounding; sorted segments (d = 16): a sequential FP32 sum of ~120,000 terms
+    assert err <= (1e-5 if d <= 8 else 1e-3) * exact.abs().max().item()

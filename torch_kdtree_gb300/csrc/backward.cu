@@ -9,7 +9,7 @@
 //   grad_ref[m] = sum_{(i,j): idx[i,j] = m} 2 g[i, j] (ref[m] - q[i])
 // grad_ref is a segmented reduction over the indices, bitwise reproducible and
 // without float atomics, in one of two forms:
-//  * float32, d <= 3: segments are built by counting (integer atomics), a
+//  * float32, d <= 8: segments are built by counting (integer atomics), a
 //    scan and an atomic fill, so the order inside a segment is arbitrary; the
 //    segment's sum is made order-independent instead.  One pass finds the
 //    largest exponent of its terms per coordinate, a second adds every FP32
@@ -107,7 +107,7 @@ __global__ void k_grad_ref(const T* __restrict__ q, const T* __restrict__ ref, c
         if (c < d) grad_ref[(long long)m * d + c] = acc[c];
 }
 
-// Segments by counting (float32, d <= 3): counts of every key, then their
+// Segments by counting (float32, d <= 8): counts of every key, then their
 // exclusive scan (n + 1 entries: starts, and the total at n).
 __global__ void k_count_keys(const int32_t* __restrict__ idx, long long npairs, int n, int* __restrict__ cnt) {
     const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -157,15 +157,16 @@ __device__ __forceinline__ long long to_fixed(float t, int sh) {
 // below 2^61, so the int64 accumulator cannot overflow.  Each scaled term is
 // rounded to an integer once (to_fixed), by a rule that does not depend on
 // the order.
+// D: compile-time bound of the runtime dimension d (d <= D <= 8).
 template <int D>
 __global__ void k_grad_ref_fixed(const float* __restrict__ q, const float* __restrict__ ref, const float* __restrict__ g,
-                                 const uint32_t* __restrict__ list, const int* __restrict__ starts, int n, int k,
+                                 const uint32_t* __restrict__ list, const int* __restrict__ starts, int n, int k, int d,
                                  float* __restrict__ grad_ref) {
     const int m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= n) return;
     float rm[D];
 #pragma unroll
-    for (int c = 0; c < D; ++c) rm[c] = ref[(long long)m * D + c];
+    for (int c = 0; c < D; ++c) rm[c] = c < d ? ref[(long long)m * d + c] : 0.f;
     const int s0 = starts[m], s1 = starts[m + 1];
     int emax[D];
 #pragma unroll
@@ -177,7 +178,7 @@ __global__ void k_grad_ref_fixed(const float* __restrict__ q, const float* __res
         const float w = 2.f * g[p];
 #pragma unroll
         for (int c = 0; c < D; ++c) {
-            const int e = exp_field(__fmul_rn(w, __fsub_rn(rm[c], q[i * D + c])));
+            const int e = exp_field(__fmul_rn(w, __fsub_rn(rm[c], (c < d ? q[i * d + c] : rm[c]))));
             finite = finite && e != 255;
             emax[c] = max(emax[c], e);
         }
@@ -192,7 +193,7 @@ __global__ void k_grad_ref_fixed(const float* __restrict__ q, const float* __res
             const long long i = (long long)(p / uint32_t(k));
             const float w = 2.f * g[p];
 #pragma unroll
-            for (int c = 0; c < D; ++c) out[c] += __fmul_rn(w, __fsub_rn(rm[c], q[i * D + c]));
+            for (int c = 0; c < D; ++c) out[c] += __fmul_rn(w, __fsub_rn(rm[c], (c < d ? q[i * d + c] : rm[c])));
         }
     } else {
         const int L = 32 - __clz(s1 - s0);  // s1 - s0 < 2^L
@@ -205,13 +206,14 @@ __global__ void k_grad_ref_fixed(const float* __restrict__ q, const float* __res
             const float w = 2.f * g[p];
 #pragma unroll
             for (int c = 0; c < D; ++c)
-                acc[c] += to_fixed(__fmul_rn(w, __fsub_rn(rm[c], q[i * D + c])), 187 - L - emax[c]);
+                acc[c] += to_fixed(__fmul_rn(w, __fsub_rn(rm[c], (c < d ? q[i * d + c] : rm[c]))), 187 - L - emax[c]);
         }
 #pragma unroll
         for (int c = 0; c < D; ++c) out[c] = float(double(acc[c]) * pow2(emax[c] + L - 187));
     }
 #pragma unroll
-    for (int c = 0; c < D; ++c) grad_ref[(long long)m * D + c] = out[c];
+    for (int c = 0; c < D; ++c)
+        if (c < d) grad_ref[(long long)m * d + c] = out[c];
 }
 
 struct BwLayout {
@@ -252,7 +254,7 @@ int run_backward(const T* q, const T* ref, const int32_t* idx, const T* g, int n
                  T* grad_ref, char* ws, cudaStream_t s) {
     const int bs = D > 32 ? 64 : 256;
     if (grad_q) k_grad_q<T, D><<<(nq + bs - 1) / bs, bs, 0, s>>>(q, ref, idx, g, nq, n, k, d, grad_q);
-    if (grad_ref && sizeof(T) == 4 && D <= 3) {
+    if (grad_ref && sizeof(T) == 4 && D <= 8) {
         const BwLayout w = bw_layout(nq, k, n);
         const long long np = (long long)nq * k;
         int* starts = reinterpret_cast<int*>(ws + w.seg_end);      // n + 1
@@ -265,11 +267,11 @@ int run_backward(const T* q, const T* ref, const int32_t* idx, const T* g, int n
         e = exclusive_scan(starts, int64_t(n) + 1, ws + w.scan_ws, s);
         if (e != cudaSuccess) return fail(TK_ECUDA, std::string("backward scan: ") + cudaGetErrorString(e));
         if (np > 0) k_fill_segments<<<unsigned((np + 255) / 256), 256, 0, s>>>(idx, np, n, starts, cursor, list);
-        if constexpr (sizeof(T) == 4 && D <= 3)
+        if constexpr (sizeof(T) == 4 && D <= 8)
             k_grad_ref_fixed<D><<<(n + 255) / 256, 256, 0, s>>>(reinterpret_cast<const float*>(q),
                                                                  reinterpret_cast<const float*>(ref),
                                                                  reinterpret_cast<const float*>(g), list, starts, n, k,
-                                                                 reinterpret_cast<float*>(grad_ref));
+                                                                 d, reinterpret_cast<float*>(grad_ref));
     } else if (grad_ref) {
         const BwLayout w = bw_layout(nq, k, n);
         const long long np = (long long)nq * k;
