@@ -84,7 +84,7 @@ def test_header_is_c99_and_links_from_c(tmp_path):
 
 
 def host_tree(points, levels):
-    from torch_kdtree_gb300._lib import LIB, TkError, check  # noqa: F401
+    from torch_kdtree_gb300._lib import LIB
     h = ctypes.c_void_p()
     dt = 0 if points.dtype == np.float32 else 1
     st = LIB.tk_tree_create(points.ctypes.data, points.shape[0], points.shape[1], dt, levels, -1, 0,

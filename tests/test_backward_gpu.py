@@ -1,7 +1,6 @@
 """The hand-written backward (tk_knn_backward) against the reference's
 torch-indexed gradient, FP64 central finite differences, and itself
 (bitwise determinism)."""
-import numpy as np
 import pytest
 import torch
 
