@@ -9,9 +9,10 @@
 //   grad_ref[m] = sum_{(i,j): idx[i,j] = m} 2 g[i, j] (ref[m] - q[i])
 // grad_ref is a segmented reduction over the indices, bitwise reproducible and
 // without float atomics, in one of two forms:
-//  * float32, d <= 8: segments are built by counting (integer atomics), a
-//    scan and an atomic fill, so the order inside a segment is arbitrary; the
-//    segment's sum is made order-independent instead.  One pass finds the
+//  * float32, d <= 8: segments are built by counting (integer atomics, whose
+//    returned ranks then place each pair), so the order inside a segment is
+//    arbitrary; the segment's sum is made order-independent instead.  One
+//    pass finds the
 //    largest exponent of its terms per coordinate, a second adds every FP32
 //    term exactly as a 64-bit fixed-point integer scaled to that exponent,
 //    and the total is rounded once -- the same bits whatever the order, and
@@ -107,23 +108,27 @@ __global__ void k_grad_ref(const T* __restrict__ q, const T* __restrict__ ref, c
         if (c < d) grad_ref[(long long)m * d + c] = acc[c];
 }
 
-// Segments by counting (float32, d <= 8): counts of every key, then their
-// exclusive scan (n + 1 entries: starts, and the total at n).
-__global__ void k_count_keys(const int32_t* __restrict__ idx, long long npairs, int n, int* __restrict__ cnt) {
+// Segments by counting (float32, d <= 8): counts of every key (then their
+// exclusive scan, n + 1 entries: starts, and the total at n), and each pair's
+// arrival rank within its key, which places it in the segment without a
+// second round of atomics.
+__global__ void k_count_keys(const int32_t* __restrict__ idx, long long npairs, int n, int* __restrict__ cnt,
+                             int* __restrict__ rank) {
     const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= npairs) return;
     const int m = idx[p];
-    if (m >= 0 && m < n) atomicAdd(cnt + m, 1);
+    rank[p] = (m >= 0 && m < n) ? atomicAdd(cnt + m, 1) : -1;
 }
 
-// Every valid pair into its key's segment, in arbitrary order.
+// Every valid pair into its key's segment (arbitrary order within it).
 __global__ void k_fill_segments(const int32_t* __restrict__ idx, long long npairs, int n,
-                                const int* __restrict__ starts, int* __restrict__ cursor, uint32_t* __restrict__ list) {
+                                const int* __restrict__ starts, const int* __restrict__ rank,
+                                uint32_t* __restrict__ list) {
     const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= npairs) return;
     const int m = idx[p];
     if (m < 0 || m >= n) return;
-    list[starts[m] + atomicAdd(cursor + m, 1)] = uint32_t(p);
+    list[starts[m] + rank[p]] = uint32_t(p);
 }
 
 // Exponent field of a float (0 for zeros and subnormals, 255 for inf / NaN).
@@ -257,16 +262,15 @@ int run_backward(const T* q, const T* ref, const int32_t* idx, const T* g, int n
     if (grad_ref && sizeof(T) == 4 && D <= 8) {
         const BwLayout w = bw_layout(nq, k, n);
         const long long np = (long long)nq * k;
-        int* starts = reinterpret_cast<int*>(ws + w.seg_end);      // n + 1
-        int* cursor = reinterpret_cast<int*>(ws + w.seg_start);    // n
+        int* starts = reinterpret_cast<int*>(ws + w.seg_end);  // n + 1
+        int* rank = reinterpret_cast<int*>(ws + w.keys);        // np
         uint32_t* list = reinterpret_cast<uint32_t*>(ws + w.sorted_vals);
         cudaError_t e = cudaMemsetAsync(starts, 0, sizeof(int) * (size_t(n) + 1), s);
-        if (e == cudaSuccess) e = cudaMemsetAsync(cursor, 0, sizeof(int) * size_t(n), s);
         if (e != cudaSuccess) return fail(TK_ECUDA, std::string("memset: ") + cudaGetErrorString(e));
-        if (np > 0) k_count_keys<<<unsigned((np + 255) / 256), 256, 0, s>>>(idx, np, n, starts);
+        if (np > 0) k_count_keys<<<unsigned((np + 255) / 256), 256, 0, s>>>(idx, np, n, starts, rank);
         e = exclusive_scan(starts, int64_t(n) + 1, ws + w.scan_ws, s);
         if (e != cudaSuccess) return fail(TK_ECUDA, std::string("backward scan: ") + cudaGetErrorString(e));
-        if (np > 0) k_fill_segments<<<unsigned((np + 255) / 256), 256, 0, s>>>(idx, np, n, starts, cursor, list);
+        if (np > 0) k_fill_segments<<<unsigned((np + 255) / 256), 256, 0, s>>>(idx, np, n, starts, rank, list);
         if constexpr (sizeof(T) == 4 && D <= 8)
             k_grad_ref_fixed<D><<<(n + 255) / 256, 256, 0, s>>>(reinterpret_cast<const float*>(q),
                                                                  reinterpret_cast<const float*>(ref),
