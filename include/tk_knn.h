@@ -164,7 +164,8 @@ int tk_tree_query(const tk_tree* tree, const void* q, int64_t nq, int k, void* d
  * Synchronous on `stream`: returns when the results are in host memory.
  * Device staging and workspace are allocated on first use and kept, grown as
  * needed, until tk_tree_destroy; calls on one tree are serialised.  Results
- * are identical to tk_tree_query's.  Replaces the host-tensor use of
+ * are identical to tk_tree_query's; device or mixed buffers work too (the
+ * copies take their direction from the pointers).  Replaces the host-tensor use of
  * TorchKDTree.query (torch_kdtree/nn_distance.py:80 copies the queries to
  * the device; the caller copies the results back). */
 int tk_tree_query_host(const tk_tree* tree, const void* q, int64_t nq, int k, void* dists, int32_t* idx,

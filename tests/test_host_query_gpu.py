@@ -109,6 +109,24 @@ def test_host_query_edge_cases():
     assert rc == _lib.TK_EINVAL
 
 
+def test_host_query_accepts_device_buffers_too():
+    """The host-buffer entry point copies with the kind inferred from the
+    pointers, so device (or mixed) buffers work as well."""
+    from torch_kdtree_gb300.nn_distance import knn_query_host
+    rng = np.random.default_rng(12)
+    ref = torch.from_numpy(rng.random((20000, 3), dtype=np.float32)).to(cuda)
+    tree = tk().build_kd_tree(ref)
+    q = torch.from_numpy(rng.random((5000, 3), dtype=np.float32))
+    dd, di = tree.query(q.to(cuda), nr_nns_searches=6)
+    d_dev = torch.empty(5000, 6, device=cuda)
+    i_dev = torch.empty(5000, 6, dtype=torch.int32, device=cuda)
+    knn_query_host(tree._tree, q.to(cuda), 6, d_dev, i_dev, cuda, tree.query_opts)
+    assert torch.equal(d_dev, dd) and torch.equal(i_dev, di)
+    d_h, i_h = host_buffers(5000, 6, torch.float32, False)
+    knn_query_host(tree._tree, q.to(cuda), 6, d_h, i_h, cuda, tree.query_opts)
+    assert torch.equal(d_h, dd.cpu()) and torch.equal(i_h, di.cpu())
+
+
 def test_host_query_waits_for_earlier_stream_work():
     """Queries copied device -> pinned host asynchronously on the current
     stream just before the call: the pipeline's uploads start after that copy."""

@@ -923,15 +923,15 @@ extern "C" int tk_tree_query_host(const tk_tree* t, const void* q, int64_t nq, i
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     cudaError_t e = cudaSuccess;
     char* dq = buf + wsb;
-    e = cudaMemcpyAsync(dq, q, qb, cudaMemcpyHostToDevice, s);
+    e = cudaMemcpyAsync(dq, q, qb, cudaMemcpyDefault, s);  // unified addressing: any kind of buffer
     if (direct) {
         if (e == cudaSuccess) rc = tk_tree_query(t, dq, nq, k, md, static_cast<int32_t*>(mi), &o, buf, wsb, s);
     } else {
         char* dd = dq + align_up(qb, 256);
         char* di = dd + align_up(db, 256);
         if (e == cudaSuccess) rc = tk_tree_query(t, dq, nq, k, dd, reinterpret_cast<int32_t*>(di), &o, buf, wsb, s);
-        if (e == cudaSuccess && rc == TK_OK) e = cudaMemcpyAsync(dists, dd, db, cudaMemcpyDeviceToHost, s);
-        if (e == cudaSuccess && rc == TK_OK) e = cudaMemcpyAsync(idx, di, ib, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess && rc == TK_OK) e = cudaMemcpyAsync(dists, dd, db, cudaMemcpyDefault, s);
+        if (e == cudaSuccess && rc == TK_OK) e = cudaMemcpyAsync(idx, di, ib, cudaMemcpyDefault, s);
     }
     const cudaError_t se = cudaStreamSynchronize(s);  // whatever was queued completes, also on failure
     if (rc != TK_OK) return rc;
