@@ -177,7 +177,25 @@ __global__ void k_grad_ref_fixed(const float* __restrict__ q, const float* __res
 #pragma unroll
     for (int c = 0; c < D; ++c) emax[c] = 0;
     bool finite = true;
-    for (int j = s0; j < s1; ++j) {
+    // d <= 3: the first kKeep terms stay in registers for the second pass
+    constexpr int kKeep = D <= 3 ? 8 : 0;
+    float keep[kKeep > 0 ? kKeep : 1][D];
+#pragma unroll
+    for (int u = 0; u < kKeep; ++u) {
+        if (s0 + u < s1) {
+            const uint32_t p = list[s0 + u];
+            const long long i = (long long)(p / uint32_t(k));
+            const float w = 2.f * g[p];
+#pragma unroll
+            for (int c = 0; c < D; ++c) {
+                keep[u][c] = __fmul_rn(w, __fsub_rn(rm[c], (c < d ? q[i * d + c] : rm[c])));
+                const int e = exp_field(keep[u][c]);
+                finite = finite && e != 255;
+                emax[c] = max(emax[c], e);
+            }
+        }
+    }
+    for (int j = s0 + kKeep; j < s1; ++j) {
         const uint32_t p = list[j];
         const long long i = (long long)(p / uint32_t(k));
         const float w = 2.f * g[p];
@@ -205,7 +223,12 @@ __global__ void k_grad_ref_fixed(const float* __restrict__ q, const float* __res
         long long acc[D];
 #pragma unroll
         for (int c = 0; c < D; ++c) acc[c] = 0;
-        for (int j = s0; j < s1; ++j) {
+#pragma unroll
+        for (int u = 0; u < kKeep; ++u)
+            if (s0 + u < s1)
+#pragma unroll
+                for (int c = 0; c < D; ++c) acc[c] += to_fixed(keep[u][c], 187 - L - emax[c]);
+        for (int j = s0 + kKeep; j < s1; ++j) {
             const uint32_t p = list[j];
             const long long i = (long long)(p / uint32_t(k));
             const float w = 2.f * g[p];
