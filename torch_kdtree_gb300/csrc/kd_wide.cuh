@@ -4,7 +4,7 @@
 // template instantiations for more (its README); the query is the same
 // algorithm at any dimension.  Trees of up to 3 dimensions keep the 16-byte
 // point records of kd_query.cuh; here, a tree of `dims` in 4..8 stores
-// W = 4 (dims 4) or 8 (dims 5-8) zero-padded coordinates per point, its
+// W = 4 (dims 4), 6 (dims 5-6) or 8 (dims 7-8) zero-padded coordinates per point, its
 // original indices in a separate array, and node boxes as lo / hi rows of W.
 // Padded coordinates are 0 in both the records and the (padded) query, so
 // each adds (0 - 0)^2 = +0 to the distance after the real terms: the sum is
@@ -65,9 +65,12 @@ __device__ __forceinline__ T sum_w(const T (&e)[W]) {
     return b;
 }
 
+// Rows start at multiples of 4 W bytes (f32) or 8 W bytes (f64) from a
+// cudaMalloc base: 16-byte loads for W = 4 and 8, 8-byte loads for W = 6 (f32).
 template <typename T, int W>
 __device__ __forceinline__ void load_row(const T* row, T (&c)[W]) {
-    if constexpr (sizeof(T) == 4) {
+    static_assert(W % 2 == 0, "rows of an even number of coordinates");
+    if constexpr (sizeof(T) == 4 && W % 4 == 0) {
 #pragma unroll
         for (int i = 0; i < W / 4; ++i) {
             const float4 v = __ldg(reinterpret_cast<const float4*>(row) + i);
@@ -75,6 +78,13 @@ __device__ __forceinline__ void load_row(const T* row, T (&c)[W]) {
             c[4 * i + 1] = v.y;
             c[4 * i + 2] = v.z;
             c[4 * i + 3] = v.w;
+        }
+    } else if constexpr (sizeof(T) == 4) {
+#pragma unroll
+        for (int i = 0; i < W / 2; ++i) {
+            const float2 v = __ldg(reinterpret_cast<const float2*>(row) + i);
+            c[2 * i] = v.x;
+            c[2 * i + 1] = v.y;
         }
     } else {
 #pragma unroll

@@ -7,6 +7,7 @@ namespace tk {
 
 #define TK_WIDE_LIST(X) \
     X(4, 1, 1) X(4, 1, 2) X(4, 1, 4) X(4, 1, 8) X(4, 1, 16) X(4, 32, 1) X(4, 32, 2) X(4, 32, 4) \
+    X(6, 1, 1) X(6, 1, 2) X(6, 1, 4) X(6, 1, 8) X(6, 1, 16) X(6, 32, 1) X(6, 32, 2) X(6, 32, 4) \
     X(8, 1, 1) X(8, 1, 2) X(8, 1, 4) X(8, 1, 8) X(8, 1, 16) X(8, 32, 1) X(8, 32, 2) X(8, 32, 4)
 
 template <>

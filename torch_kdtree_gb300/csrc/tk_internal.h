@@ -18,7 +18,7 @@ constexpr int kMaxDims = 8;      // KD-tree dimensions (brute force: up to 128)
 // Coordinates per device point record of a tree of `dims` dimensions: up to
 // 3 share one 16-byte record with the original index; 4 or 5-8 dimensions use
 // 4 or 8 zero-padded coordinates with the indices in a separate array.
-inline int record_width(int dims) { return dims <= 3 ? 3 : (dims <= 4 ? 4 : 8); }
+inline int record_width(int dims) { return dims <= 3 ? 3 : (dims <= 4 ? 4 : (dims <= 6 ? 6 : 8)); }
 
 // Sets the thread-local error text and returns the status.
 int fail(int status, const std::string& msg);
