@@ -248,8 +248,12 @@ size_t tk_knn_backward_workspace_size(int64_t nq, int k, int64_t n);
  * q [nq,dims], ref [n,dims] (1 <= dims <= 128), idx int32 [nq,k] (original indices; entries
  * outside [0,n) are skipped), grad_dists [nq,k]; grad_q [nq,dims] and
  * grad_ref [n,dims] are overwritten; either may be NULL to skip it.  The ref
- * gradient is a stable-sort + fixed-order segmented reduction: bitwise
- * identical run to run.  nq * k < 2^31.
+ * gradient is a segmented reduction over idx, bitwise identical run to run
+ * without float atomics: for float32 with dims <= 8 each segment's terms are
+ * summed exactly as 64-bit fixed-point integers scaled to the segment's
+ * largest exponent (order-independent, one final rounding); otherwise the
+ * segments come from a stable sort and are summed in pair order.
+ * nq * k < 2^31.
  * Replaces the torch re-gather + autograd of torch_kdtree/nn_distance.py:111-112
  * (index_put_ with accumulate, float atomics). */
 int tk_knn_backward(const void* q, const void* ref, const int32_t* idx, const void* grad_dists, int64_t nq,
