@@ -6,9 +6,11 @@
 // candidate is inserted serially with a block barrier.
 //
 // What this file does instead:
-//  1. Queries are first binned by the tree cell they fall into (a counting
-//     sort over the cells at depth B), so neighbouring lanes follow nearly
-//     the same path through the tree and hit the same leaves in L1.
+//  1. Calls of at least a wave of queries (SMs x 1024) first bin them by the
+//     tree cell they fall into (a counting sort over the cells at depth B), so
+//     neighbouring lanes follow nearly the same path through the tree and hit
+//     the same leaves in L1; smaller calls keep the input order (see
+//     prepare_order in tk_api.cu).
 //  2. A group of G lanes (G = 1..32, "threads per query") serves one query.
 //     The walk is a depth-first descent with an explicit short stack of far
 //     siblings; each entry carries the per-axis squared plane distances of
