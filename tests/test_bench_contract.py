@@ -1,0 +1,38 @@
+"""Host-side pieces of bench.py that need no GPU: the roofline inputs read
+from the committed ncu summaries, and the algorithmic byte count."""
+import importlib.util
+import os
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def bench():
+    spec = importlib.util.spec_from_file_location("bench_mod", os.path.join(ROOT, "bench.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def test_roofline_inputs_come_from_the_committed_profile():
+    b = bench()
+    tag = "kd_query_cube_sphere_4M_k16"
+    traffic = b.profiled_traffic(tag)
+    inst = b.profiled_value(tag, "warp_instructions_per_launch")
+    assert isinstance(traffic, int) and traffic > 100_000_000
+    assert isinstance(inst, int) and inst > 1_000_000_000
+    assert b.profiled_traffic("no_such_profile") is None
+
+
+def test_algorithmic_bytes_of_the_headline_launch():
+    b = bench()
+    # 1,048,576 queries x (12 B in + 128 B out) + 4,194,304 records x 16 B + tree arrays at depth 18
+    got = b.algorithmic_bytes(4_194_304, 1_048_576, 16, 18)
+    assert got == 1_048_576 * 140 + 4_194_304 * 16 + 4 * ((1 << 18) - 1) + 4 * ((1 << 18) + 1)
+    assert 215e6 < got < 217e6
+
+
+def test_every_profile_names_its_command():
+    for f in sorted(os.listdir(os.path.join(ROOT, "profiles"))):
+        text = open(os.path.join(ROOT, "profiles", f)).read()
+        assert f.endswith(".md")
+        assert "python bench.py" in text and "--clock-control none" in text, f
