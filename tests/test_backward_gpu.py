@@ -130,3 +130,13 @@ def test_hub_segments_are_deterministic_and_accurate(d):
     err = (outs[0].double() - exact).abs().max().item()
     # fixed-point sums: one rounding; sorted segments (d = 16): a sequential FP32 sum of ~120,000 terms
     assert err <= (1e-5 if d <= 8 else 1e-3) * exact.abs().max().item()
+
+
+def test_no_queries_gives_zero_reference_gradient():
+    from torch_kdtree_gb300.autograd import knn_backward
+    ref = torch.randn(100, 3, device=cuda)
+    q = torch.empty(0, 3, device=cuda)
+    idx = torch.empty(0, 4, dtype=torch.int32, device=cuda)
+    g = torch.empty(0, 4, device=cuda)
+    gq, gr = knn_backward(q, ref, idx, g, True, True)
+    assert gq.shape == (0, 3) and torch.equal(gr, torch.zeros_like(ref))

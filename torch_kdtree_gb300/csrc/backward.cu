@@ -281,7 +281,7 @@ template <typename T, int D>
 int run_backward(const T* q, const T* ref, const int32_t* idx, const T* g, int nq, int n, int k, int d, T* grad_q,
                  T* grad_ref, char* ws, cudaStream_t s) {
     const int bs = D > 32 ? 64 : 256;
-    if (grad_q) k_grad_q<T, D><<<(nq + bs - 1) / bs, bs, 0, s>>>(q, ref, idx, g, nq, n, k, d, grad_q);
+    if (grad_q && nq > 0) k_grad_q<T, D><<<(nq + bs - 1) / bs, bs, 0, s>>>(q, ref, idx, g, nq, n, k, d, grad_q);
     if (grad_ref && sizeof(T) == 4 && D <= 8) {
         const BwLayout w = bw_layout(nq, k, n);
         const long long np = (long long)nq * k;
@@ -345,7 +345,7 @@ int tk_knn_backward(const void* q, const void* ref, const int32_t* idx, const vo
     if (dims < 1 || dims > 128) return fail(TK_EINVAL, "dims must be in [1, 128]");
     if (dtype != TK_F32 && dtype != TK_F64) return fail(TK_EINVAL, "dtype must be TK_F32 or TK_F64");
     if (nq == 0 && !grad_ref) return TK_OK;
-    if (!q || !ref || !idx || !grad_dists) return fail(TK_EINVAL, "null input pointer");
+    if (!ref || (nq > 0 && (!q || !idx || !grad_dists))) return fail(TK_EINVAL, "null input pointer");
     if (grad_ref && (!workspace || workspace_bytes < bw_layout(nq, k, n).total))
         return fail(TK_EWORKSPACE, "workspace too small");
     if (ws_misaligned(workspace)) return fail(TK_EINVAL, "workspace must be 256-byte aligned");
