@@ -80,3 +80,22 @@ def test_fp64_helpers(oracle):
     bd, bi = oracle.brute(ref, q, 5)
     assert (i64 == bi).mean() > 0.99
     np.testing.assert_allclose(oracle.recompute_f64(ref, q, bi), bd, rtol=1e-5)
+
+
+@pytest.mark.parametrize("case", [c for c in CASES if c[3] <= 10000], ids=lambda c: c[0])
+def test_fixtures_regenerate_from_the_reference(case, oracle, golden):
+    """Where the reference's own CPU code is built (oracle/_ref, compiled from
+    its sources in the checkout), every fixture regenerates bit for bit:
+    inputs, layout and query outputs."""
+    if not oracle.ref_available():
+        pytest.skip("reference sources are not built here")
+    from make_golden import golden_inputs
+    name, dtype, d, n, nq, k, levels, kind, full = case
+    ref, q = golden_inputs(name, dtype, d, n, nq, kind)
+    tree = oracle.RefTree(ref, levels)
+    lay = tree.layout()
+    dists, idx = tree.query(q, k)
+    z = golden[name]
+    assert str(z["input_sha"]) == digest(ref, q)
+    assert str(z["layout_sha"]) == digest(lay.structured, lay.perm, lay.medians, lay.axes, lay.leaf_off, lay.leaf_cnt)
+    assert str(z["output_sha"]) == digest(dists, idx)
