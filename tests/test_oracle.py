@@ -99,3 +99,27 @@ def test_fixtures_regenerate_from_the_reference(case, oracle, golden):
     assert str(z["input_sha"]) == digest(ref, q)
     assert str(z["layout_sha"]) == digest(lay.structured, lay.perm, lay.medians, lay.axes, lay.leaf_off, lay.leaf_cnt)
     assert str(z["output_sha"]) == digest(dists, idx)
+
+
+@pytest.mark.parametrize("d", [1, 2, 3, 4, 5, 6, 7, 8])
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_restatement_equals_reference_on_fresh_clouds(d, dtype, oracle):
+    """Beyond the fixtures: on fresh tie-free clouds the C restatement and the
+    reference's own CPU code (where built) give the same layout and the same
+    query answers bit for bit, at several depths and k."""
+    if not oracle.ref_available():
+        pytest.skip("reference sources are not built here")
+    rng = np.random.default_rng(500 + 10 * d + (dtype == np.float64))
+    ref = (rng.standard_normal((3000, d)) * 1e3).astype(dtype)
+    q = (rng.standard_normal((400, d)) * 1e3).astype(dtype)
+    for levels, k in ((1, 3), (4, 9), (7, 17)):
+        mine = oracle.build_tree(ref, levels)
+        theirs = oracle.RefTree(ref, levels)
+        lay = theirs.layout()
+        np.testing.assert_array_equal(mine.structured, lay.structured)
+        np.testing.assert_array_equal(mine.perm, lay.perm)
+        np.testing.assert_array_equal(mine.medians, lay.medians)
+        d1, i1 = oracle.query_tree(mine, q, k)
+        d2, i2 = theirs.query(q, k)
+        np.testing.assert_array_equal(d1, d2)
+        np.testing.assert_array_equal(i1, i2)
