@@ -262,3 +262,14 @@ def test_layout_round_trip_and_validation(dtype, d):
     wrong_split[0] = pts[:, 0].max() + 1
     assert refused(m=wrong_split)
     assert not refused(lv=L)
+
+
+@pytest.mark.parametrize("device", ["cuda", "cpu"])
+def test_uncompiled_dimension_raises_before_any_device_work(device):
+    """The reference's test_uncompiled_dimension (tests/test_knn_unit.py:72-77):
+    436 dimensions must raise, for either device string; here the check runs
+    before anything touches a GPU (KD trees take 1-8 dimensions, and only CUDA
+    trees exist)."""
+    from torch_kdtree_gb300 import build_kd_tree
+    with pytest.raises(RuntimeError):
+        build_kd_tree(np.random.uniform(size=(10, 436)), device=device)
