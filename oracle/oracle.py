@@ -31,10 +31,14 @@ _c_i32p = ctypes.POINTER(ctypes.c_int32)
 _c_u8p = ctypes.POINTER(ctypes.c_uint8)
 
 
-def build(ref: bool = False) -> None:
-    """Compile liboracle.so (and, if asked and possible, the reference)."""
+def build(ref: bool | str = False) -> None:
+    """Compile liboracle.so and, with ref=True, the reference's own CPU
+    sources (oracle/_ref); ref="if-present" builds the latter only where the
+    Makefile's REF_SRC (environment variable TK_REFERENCE_SRC) holds them."""
     subprocess.run(["make", "-s", "-C", HERE], check=True)
-    if ref:
+    if ref == "if-present":
+        subprocess.run(["make", "-s", "-C", HERE, "ref-if-present"], check=True)
+    elif ref:
         subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
 
 

@@ -37,7 +37,7 @@ CASES = [
       for (dt, d, n, nq, k) in (("f32", 4, 1000, 200, 10), ("f32", 5, 10000, 300, 20), ("f32", 8, 10000, 300, 16),
                                 ("f64", 6, 1000, 200, 10), ("f64", 8, 5000, 200, 33), ("f32", 7, 30, 20, 5))],
     ("wide_ties_f32_d4_grid", "f32", 4, 2000, 300, 8, None, "intgrid", True),
-    # BASELINE config 1: N(0,1)*1e3, 100,000 refs, 10,000 queries, k=5, levels 13
+    # the plain workload: N(0,1)*1e3, 100,000 refs, 10,000 queries, k=5, levels 13
     ("config1_f32_d3_n100000_q10000_k5", "f32", 3, 100000, 10000, 5, None, "normal1e3", False),
 ]
 

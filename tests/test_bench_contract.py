@@ -1,6 +1,7 @@
 """Host-side pieces of bench.py that need no GPU: the roofline inputs read
 from the committed ncu summaries, and the algorithmic byte count."""
 import importlib.util
+import json
 import os
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -36,3 +37,29 @@ def test_every_profile_names_its_command():
         text = open(os.path.join(ROOT, "profiles", f)).read()
         assert f.endswith(".md")
         assert "python bench.py" in text and "--clock-control none" in text, f
+
+
+def test_reference_arm_maps_no_library_of_this_package():
+    """`bench.py --impl reference` times the reference's CPU query path; it
+    must not import this package or map its CUDA library (only the
+    oracle's libraries), so the two arms stay separate programs."""
+    import subprocess
+    import sys
+    code = (
+        "import importlib.util, os, sys, types\n"
+        f"root = {ROOT!r}\n"
+        "sys.path.insert(0, root)\n"
+        "spec = importlib.util.spec_from_file_location('bench_mod', os.path.join(root, 'bench.py'))\n"
+        "b = importlib.util.module_from_spec(spec); spec.loader.exec_module(b)\n"
+        "b.run_reference(types.SimpleNamespace(ref_sample=512, steps=1, warmup=0, gpus=1))\n"
+        "maps = open('/proc/self/maps').read()\n"
+        "assert 'libtkknn' not in maps, 'the reference arm mapped libtkknn.so'\n"
+        "bad = [m for m in sys.modules if m.startswith('torch_kdtree_gb300')]\n"
+        "assert not bad, bad\n"
+        "assert 'liboracle' in maps or 'libtkref' in maps\n"
+        "print('REFERENCE_ARM_OK')\n")
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    assert "REFERENCE_ARM_OK" in r.stdout
+    line = json.loads([ln for ln in r.stdout.splitlines() if ln.startswith("{")][-1])
+    assert line["impl"] == "reference" and line["e2e"]["h2d_bytes_per_step"] == 0
