@@ -129,8 +129,9 @@ typedef struct tk_query_opts {
     int32_t blocks_per_sm;     /* 0 = as many as fit */
     void* kernel_start_event;  /* optional cudaEvent_t recorded right before the KD kernel */
     void* kernel_stop_event;   /* optional cudaEvent_t recorded right after it */
-    int32_t prune_boxes;       /* -1 = auto (on), 0 = split planes only, 1 = also node bounding boxes */
-    int32_t traversal;         /* 0 = auto (per-query), 1 = per-query stacks (G lanes per query),
+    int32_t prune_boxes;       /* trees of 4-8 dims: -1 = auto (on), 0 = split planes only, 1 = also
+                                  node bounding boxes; trees of 1-3 dims always prune with both */
+    int32_t traversal;         /* 0 = auto (per-query), 1 = per-query search (G lanes per query),
                                   2 = warp packets: the 32 queries of a warp walk the tree together,
                                   one lane each, pruning with node boxes (k <= 16; larger k falls
                                   back to 1; threads_per_query and prune_boxes are then ignored) */
@@ -180,7 +181,7 @@ int tk_tree_query_host(const tk_tree* tree, const void* q, int64_t nq, int k, vo
  * another allocator, plain C/FFI callers with no device allocator of their
  * own, and latency-critical code where cudaMalloc (which synchronises the
  * device) is not acceptable.  Scratch comes from a static device array of
- * about 3.3 MiB built into the library (held on every GPU that loads it until
+ * about 4.4 MiB built into the library (held on every GPU that loads it until
  * the process exits).  At most TK_NOALLOC_MAX_QUERIES queries per call; more
  * fails with TK_EINVAL.  Every call on a device shares that array: calls that
  * may overlap on the GPU (different streams, or threads without ordering)
@@ -211,8 +212,8 @@ int64_t tk_batch_output_size(const tk_batch* batch);
 /* All clouds in one persistent launch fed by a global work counter (plus
  * the binning kernels).  Device work only, no host synchronisation and no
  * allocation: it can be captured in a CUDA graph.  threads_per_query: 0 =
- * auto, 1 (max k <= 16) or 8.  prune_boxes: 0 = split planes only, 1 = also
- * node bounding boxes (as in tk_query_opts). */
+ * auto, 1 (max k <= 16) or 8.  prune_boxes: ignored (kept for binary
+ * compatibility): the batched search always prunes with node bounding boxes. */
 int tk_batch_query(const tk_batch* batch, const void* q, void* dists, int32_t* idx, int threads_per_query,
                    int prune_boxes, void* workspace, size_t workspace_bytes, void* stream);
 

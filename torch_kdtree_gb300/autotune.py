@@ -108,7 +108,8 @@ def autotune(points_ref: torch.Tensor, queries: torch.Tensor, k: int,
         # a lane holds <= 16 keys; trees of more than 3 dims run 1 or 32 lanes per
         # query and the per-query-stack traversal only
         shapes = [g for g in lanes if g * 16 >= k and (d <= 3 or g in (1, 32))]
-        cands = [(g, boxes, 1) for g in shapes for boxes in (1, 0)]
+        # node-box pruning is an option for trees of 4-8 dims only (1-3 dims always prune with boxes)
+        cands = [(g, boxes, 1) for g in shapes for boxes in ((1, 0) if d > 3 else (1,))]
         if k <= 16 and d <= 3:
             cands.append((1, 1, 2))  # warp packets
         for g, boxes, trav in cands:

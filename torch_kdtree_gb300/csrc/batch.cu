@@ -85,7 +85,7 @@ __global__ void k_batch_bin_count(const BatchArgs<T> a, int* counts, int* bin_of
 template <typename T, int D, int G, int R>
 __device__ __forceinline__ void batch_search(const CloudDesc<T>& cd, const T (&q)[D], long long local,
                                              const BatchArgs<T>& a, unsigned gmask, int gl, int gbase) {
-    const TreeView<T> tv{cd.pts, cd.medians, cd.leaf_off, cd.levels, 0, nullptr, a.use_boxes ? cd.boxes : nullptr};
+    const TreeView<T> tv{cd.pts, cd.medians, cd.leaf_off, cd.levels, 0, nullptr, cd.boxes};
     const long long o = cd.out_off + local * cd.k;
     kd_search<T, D, G, R>(tv, q, cd.k, a.out_d + o, a.out_i + o, gmask, gl, gbase);
 }

@@ -59,17 +59,17 @@ struct KdArgs {
 };
 
 template <typename T, int D>
-struct StackEntry {
-    int node;
-    T e[D];  // per-axis squared distance from the query to the cell's slab
-};
-
-template <typename T, int D>
 __device__ __forceinline__ T cell_bound(const T (&e)[D]) {
     T b = e[0];
     if (D > 1) b = add_rn(b, e[1]);
     if (D > 2) b = add_rn(b, e[2]);
     return b;
+}
+
+// Value of lane `src` of a G-lane group (every lane of the group calls it).
+template <typename T, int G>
+__device__ __forceinline__ T shfl_group(unsigned gmask, T v, int src) {
+    return __shfl_sync(gmask, v, src, G);
 }
 
 template <typename T, int D>
@@ -142,6 +142,20 @@ __device__ __forceinline__ void bitonic_sort(Key<T> (&v)[R]) {
 
 // Exhaustive-equivalent KNN for one query, served by a group of G lanes;
 // writes k results to out_d[0..k) / out_i[0..k).
+//
+// Depth-first search without a stack in memory.  The path from the root to
+// the current leaf is the leaf's heap index, so a far sibling still to visit
+// needs one bit: bit t of `pending` says "the sibling of the path node at
+// depth t + 1 may hold a neighbour".  After a leaf the deepest pending bit is
+// taken first (the same order a stack would give); the sibling's id follows
+// from the leaf id by shifts.  A pending sibling is checked against the
+// current k-th distance twice, cheapest first -- groups of 8 or more lanes
+// by the bound of its cell recorded when it was marked (one register per
+// depth, spread over the group's lanes: depth t lives in lane t % G),
+// smaller groups by its parent's split plane (top levels in shared memory)
+// -- then by its bounding box, whose per-axis gaps also become the axis
+// bounds its own descent starts from.  All lanes of a group hold the same
+// trail: no local memory, for any group size.
 template <typename T, int D, int G, int R>
 __device__ __forceinline__ void kd_search(const TreeView<T>& tv, const T (&q)[D], int k, T* out_d,
                                           int32_t* out_i, unsigned gmask, int gl, int gbase) {
@@ -149,109 +163,151 @@ __device__ __forceinline__ void kd_search(const TreeView<T>& tv, const T (&q)[D]
     list.init(k, gl);
     Key<T> worst = Key<T>::sentinel();
     T worst_d = worst.dist();
-
-    StackEntry<T, D> stk[kMaxLevels];
-    int sp = 0;
-    int node = 0, depth = 0;
-    bool home = true;  // the first leaf reached is the query's own cell
-    T e[D];
-#pragma unroll
-    for (int c = 0; c < D; ++c) e[c] = T(0);
     const int L = tv.levels;
-    const int first_leaf = (1 << L) - 1;
+
+    // recorded cell bounds of pending siblings (groups of >= 8 lanes): depth t
+    // in register t / G of lane t % G
+    constexpr int NB = G >= 8 ? (kMaxLevels + G - 1) / G : 0;
+    T pb[NB > 0 ? NB : 1];
+
+    // the home leaf: the cell the query falls into (src/kdtree.cpp:30 rule);
+    // a sibling on the home path is bounded by its split plane alone
+    int node = 0;
+    for (int depth = 0, ax = 0; depth < L; ++depth) {
+        const T m = depth < tv.smem_levels ? tv.s_med[node] : __ldg(tv.medians + node);
+        const T qa = pick<T, D>(q, ax);
+        if constexpr (NB > 0) {
+            const T diff = sub_rn(qa, m);
+            if (gl == depth % G) {
+#pragma unroll
+                for (int j = 0; j < NB; ++j)
+                    if (depth / G == j) pb[j] = mul_rn(diff, diff);
+            }
+        }
+        node = 2 * node + (qa < m ? 1 : 2);
+        ax = (ax + 1 == D) ? 0 : ax + 1;
+    }
+    uint32_t pending = (1u << L) - 1u;  // every far sibling on the home path (L <= 24)
+    bool home = true;
 
     for (;;) {
-        // descend to the near leaf, stacking far siblings that may matter
+        // `node` is a leaf; its box records carry its point range (one round trip for both)
+        {
+            const PointRec<T> lo = load_rec(tv.boxes + 2 * node);
+            const PointRec<T> hi = load_rec(tv.boxes + 2 * node + 1);
+            int beg = int(rec_index(lo));
+            const int end = int(rec_index(hi));
+            if (box_bound_of<T, D>(lo, hi, q) <= worst_d) {
+                if (G == 1 && home && k == R && end - beg >= R) {
+                    // fill the whole list from the home cell with one sorting
+                    // network instead of R single insertions
+                    Key<T> v[R];
+#pragma unroll
+                    for (int i = 0; i < R; ++i) {
+                        const PointRec<T> p = load_rec(tv.pts + beg + i);
+                        v[i] = Key<T>::make(sqdist<T, D>(q, p), rec_index(p));
+                    }
+                    bitonic_sort<T, R>(v);
+#pragma unroll
+                    for (int i = 0; i < R; ++i) list.slot[i] = v[i];
+                    worst = list.worst(gmask);
+                    beg += R;
+                }
+                if constexpr (G == 1) {
+                    // two records per step: independent loads and distance chains
+                    int j = beg;
+                    for (; j + 1 < end; j += 2) {
+                        const PointRec<T> p0 = load_rec(tv.pts + j);
+                        const PointRec<T> p1 = load_rec(tv.pts + j + 1);
+                        const Key<T> k0 = Key<T>::make(sqdist<T, D>(q, p0), rec_index(p0));
+                        const Key<T> k1 = Key<T>::make(sqdist<T, D>(q, p1), rec_index(p1));
+                        worst = offer<T, G, R>(list, k0, worst, gmask, gl, gbase);
+                        worst = offer<T, G, R>(list, k1, worst, gmask, gl, gbase);
+                    }
+                    if (j < end) {
+                        const PointRec<T> p = load_rec(tv.pts + j);
+                        worst = offer<T, G, R>(list, Key<T>::make(sqdist<T, D>(q, p), rec_index(p)), worst, gmask,
+                                               gl, gbase);
+                    }
+                } else {
+                    for (int j0 = beg; j0 < end; j0 += G) {
+                        const int j = j0 + gl;
+                        Key<T> mine = Key<T>::sentinel();
+                        if (j < end) {
+                            const PointRec<T> p = load_rec(tv.pts + j);
+                            mine = Key<T>::make(sqdist<T, D>(q, p), rec_index(p));
+                        }
+                        worst = offer<T, G, R>(list, mine, worst, gmask, gl, gbase);
+                    }
+                }
+                worst_d = worst.dist();
+            }
+        }
+        home = false;
+
+        // the deepest pending far sibling that can still hold a neighbour
+        // (bounds are compared as !(b <= worst) so a NaN bound prunes)
+        T e[D];
+        int depth = 0;
+        while (pending) {
+            const int t = 31 - __clz(pending);
+            pending ^= 1u << t;
+            const int a = ((node + 1) >> (L - 1 - t)) - 1;  // path node at depth t + 1
+            const int far = ((a + 1) ^ 1) - 1;              // its sibling
+            if constexpr (NB > 0) {
+                T v = pb[0];
+#pragma unroll
+                for (int j = 1; j < NB; ++j) v = (t / G == j) ? pb[j] : v;
+                if (!(shfl_group<T, G>(gmask, v, t % G) <= worst_d)) continue;
+            } else {
+                const int parent = (a - 1) >> 1;
+                const T m = t < tv.smem_levels ? tv.s_med[parent] : __ldg(tv.medians + parent);
+                const T diff = sub_rn(pick<T, D>(q, t % D), m);
+                if (!(mul_rn(diff, diff) <= worst_d)) continue;
+            }
+            const PointRec<T> lo = load_rec(tv.boxes + 2 * far);
+            const PointRec<T> hi = load_rec(tv.boxes + 2 * far + 1);
+            const T l[3] = {lo.x, lo.y, lo.z};
+            const T h[3] = {hi.x, hi.y, hi.z};
+#pragma unroll
+            for (int c = 0; c < D; ++c) {
+                const T g = q[c] < l[c] ? sub_rn(q[c], l[c]) : (q[c] > h[c] ? sub_rn(q[c], h[c]) : T(0));
+                e[c] = mul_rn(g, g);
+            }
+            if (!(cell_bound<T, D>(e) <= worst_d)) continue;
+            node = far;
+            depth = t + 1;
+            break;
+        }
+        if (depth == 0) break;
+
+        // descend to the near leaf; a far child becomes pending when the
+        // bound of its cell (this cell's axis bounds, the split plane on its
+        // axis) is within reach
         int ax = depth % D;
         while (depth < L) {
             const T m = depth < tv.smem_levels ? tv.s_med[node] : __ldg(tv.medians + node);
             const T qa = pick<T, D>(q, ax);
             const T diff = sub_rn(qa, m);
             const T plane = mul_rn(diff, diff);
-            const bool go_left = qa < m;  // src/kdtree.cpp:30
-            StackEntry<T, D> far;
-            far.node = 2 * node + (go_left ? 2 : 1);
+            T fe[D];
 #pragma unroll
-            for (int c = 0; c < D; ++c) far.e[c] = (c == ax) ? plane : e[c];
-            if (cell_bound<T, D>(far.e) <= worst_d) stk[sp++] = far;
-            node = 2 * node + (go_left ? 1 : 2);
+            for (int c = 0; c < D; ++c) fe[c] = (c == ax) ? plane : e[c];
+            const T fb = cell_bound<T, D>(fe);
+            if (fb <= worst_d) {
+                pending |= 1u << depth;
+                if constexpr (NB > 0) {
+                    if (gl == depth % G) {
+#pragma unroll
+                        for (int j = 0; j < NB; ++j)
+                            if (depth / G == j) pb[j] = fb;
+                    }
+                }
+            }
+            node = 2 * node + (qa < m ? 1 : 2);  // src/kdtree.cpp:30
             ++depth;
             ax = (ax + 1 == D) ? 0 : ax + 1;
         }
-        // scan the leaf bucket, G points at a time (unless its box is out of reach)
-        // (a leaf's box records carry its point range: one round trip for both)
-        int beg, end;
-        bool scan = true;
-        if (tv.boxes) {
-            const PointRec<T> lo = load_rec(tv.boxes + 2 * node);
-            const PointRec<T> hi = load_rec(tv.boxes + 2 * node + 1);
-            scan = box_bound_of<T, D>(lo, hi, q) <= worst_d;
-            beg = int(rec_index(lo));
-            end = int(rec_index(hi));
-        } else {
-            beg = __ldg(tv.leaf_off + (node - first_leaf));
-            end = __ldg(tv.leaf_off + (node - first_leaf) + 1);
-        }
-        if (scan) {
-            if (G == 1 && home && k == R && end - beg >= R) {
-                // fill the whole list from the home cell with one sorting
-                // network instead of R single insertions
-                Key<T> v[R];
-#pragma unroll
-                for (int i = 0; i < R; ++i) {
-                    const PointRec<T> p = load_rec(tv.pts + beg + i);
-                    v[i] = Key<T>::make(sqdist<T, D>(q, p), rec_index(p));
-                }
-                bitonic_sort<T, R>(v);
-#pragma unroll
-                for (int i = 0; i < R; ++i) list.slot[i] = v[i];
-                worst = list.worst(gmask);
-                beg += R;
-            }
-            if constexpr (G == 1) {
-                // two records per step: independent loads and distance chains
-                int j = beg;
-                for (; j + 1 < end; j += 2) {
-                    const PointRec<T> p0 = load_rec(tv.pts + j);
-                    const PointRec<T> p1 = load_rec(tv.pts + j + 1);
-                    const Key<T> k0 = Key<T>::make(sqdist<T, D>(q, p0), rec_index(p0));
-                    const Key<T> k1 = Key<T>::make(sqdist<T, D>(q, p1), rec_index(p1));
-                    worst = offer<T, G, R>(list, k0, worst, gmask, gl, gbase);
-                    worst = offer<T, G, R>(list, k1, worst, gmask, gl, gbase);
-                }
-                if (j < end) {
-                    const PointRec<T> p = load_rec(tv.pts + j);
-                    worst = offer<T, G, R>(list, Key<T>::make(sqdist<T, D>(q, p), rec_index(p)), worst, gmask, gl,
-                                           gbase);
-                }
-            } else {
-                for (int j0 = beg; j0 < end; j0 += G) {
-                    const int j = j0 + gl;
-                    Key<T> mine = Key<T>::sentinel();
-                    if (j < end) {
-                        const PointRec<T> p = load_rec(tv.pts + j);
-                        mine = Key<T>::make(sqdist<T, D>(q, p), rec_index(p));
-                    }
-                    worst = offer<T, G, R>(list, mine, worst, gmask, gl, gbase);
-                }
-            }
-            worst_d = worst.dist();
-        }
-        home = false;
-        // resume at the deepest stacked cell that can still hold a neighbour
-        bool resumed = false;
-        while (sp > 0) {
-            const StackEntry<T, D> s = stk[--sp];
-            if (cell_bound<T, D>(s.e) <= worst_d && (!tv.boxes || box_bound<T, D>(tv.boxes, s.node, q) <= worst_d)) {
-                node = s.node;
-#pragma unroll
-                for (int c = 0; c < D; ++c) e[c] = s.e[c];
-                depth = 31 - __clz(node + 1);
-                resumed = true;
-                break;
-            }
-        }
-        if (!resumed) break;
     }
     list.store(k, gl, out_d, out_i, 0);
 }
@@ -450,28 +506,62 @@ __global__ void __launch_bounds__(256) k_kd_packet(const KdArgs<T> a) {
 
 // ---------------------------------------------------------- query binning --
 
-// Cell id at depth B of every query (same descent rule as the search) and
-// its arrival rank within the cell.
+// Cost class of a query for the launch order (smaller = costlier).  The
+// squared distance from the query to the farthest corner of its home leaf's
+// bounding box bounds its distance to every point of that leaf, so it tracks
+// the radius the search must cover: queries far from their leaf's points
+// (outside the cloud, in sparse regions) scan many more leaves.  Its float
+// exponent and top mantissa bit give half-octave classes, 2^-63 .. 2^64
+// mapped onto 255 .. 0; an empty leaf or a non-finite value gets the last
+// class.
+__device__ __forceinline__ uint32_t cost_class(float far2) {
+    if (!(far2 <= 3.0e38f)) return 255u;
+    const uint32_t bucket = __float_as_uint(far2) >> 22;  // exponent and top mantissa bit
+    const uint32_t c = bucket < 128u ? 0u : (bucket - 128u > 255u ? 255u : bucket - 128u);
+    return 255u - c;
+}
+
+// Cell id at depth B of every query (same descent rule as the search), its
+// arrival rank within the cell, and (with `boxes`) its cost class from the
+// home leaf at depth L: bin_of = cell | class << 16 (B <= 16).
 template <typename T, int D>
-__global__ void k_bin_count(const T* __restrict__ q, int nq, const T* __restrict__ medians, int B,
-                            int* __restrict__ counts, int* __restrict__ bin_of, int* __restrict__ pos_of) {
+__global__ void k_bin_count(const T* __restrict__ q, int nq, const T* __restrict__ medians, int B, int L,
+                            const PointRec<T>* __restrict__ boxes, int* __restrict__ counts,
+                            int* __restrict__ bin_of, int* __restrict__ pos_of) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nq) return;
     T p[D];
 #pragma unroll
     for (int c = 0; c < D; ++c) p[c] = q[(long long)i * D + c];
-    int node = 0, ax = 0;
-    for (int depth = 0; depth < B; ++depth) {
+    int node = 0, ax = 0, bin = 0;
+    const int stop = boxes ? L : B;
+    for (int depth = 0; depth < stop; ++depth) {
+        if (depth == B) bin = node - ((1 << B) - 1);
         const T m = __ldg(medians + node);
         node = 2 * node + (pick<T, D>(p, ax) < m ? 1 : 2);
         ax = (ax + 1 == D) ? 0 : ax + 1;
     }
-    const int bin = node - ((1 << B) - 1);
-    bin_of[i] = bin;
+    if (stop == B) bin = node - ((1 << B) - 1);
+    uint32_t cls = 0;
+    if (boxes) {
+        const PointRec<T> lo = load_rec(boxes + 2 * node);
+        const PointRec<T> hi = load_rec(boxes + 2 * node + 1);
+        const T l[3] = {lo.x, lo.y, lo.z};
+        const T h[3] = {hi.x, hi.y, hi.z};
+        float far2 = 0.f;
+#pragma unroll
+        for (int c = 0; c < D; ++c) {
+            const float f = float(fmax(fabs(p[c] - l[c]), fabs(p[c] - h[c])));
+            far2 += f * f;
+        }
+        cls = cost_class(far2);
+    }
+    bin_of[i] = bin | int(cls << 16);
     pos_of[i] = atomicAdd(counts + bin, 1);
 }
 
-__global__ void k_bin_scatter(int nq, const int* bin_of, const int* pos_of, const int* offsets, int* order);
+__global__ void k_bin_scatter(int nq, const int* bin_of, const int* pos_of, const int* offsets, int* order,
+                              uint32_t* classes);
 
 // Per-(T, D) launcher implemented in kd_query_<type>_d<D>.cu.
 struct KdLaunch {
@@ -488,7 +578,7 @@ int kd_packet_launch(const KdArgs<T>& a, const KdLaunch& l, cudaStream_t s);  //
 template <typename T, int D>
 const void* kd_packet_kernel(int R);
 template <typename T, int D>
-void bin_count_launch(const T* q, int nq, const T* medians, int B, int* counts, int* bin_of, int* pos_of,
-                      cudaStream_t s);
+void bin_count_launch(const T* q, int nq, const T* medians, int B, int L, const PointRec<T>* boxes, int* counts,
+                      int* bin_of, int* pos_of, cudaStream_t s);
 
 }  // namespace tk

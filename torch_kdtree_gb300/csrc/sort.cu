@@ -182,6 +182,28 @@ size_t sort_workspace_bytes(int64_t n) {
            2 * align256(sizeof(uint32_t) * size_t(std::max<int64_t>(n, 1)));
 }
 
+size_t sort_pass8_workspace_bytes(int64_t n) {
+    const int64_t ntiles = std::max<int64_t>(1, (n + kTile - 1) / kTile);
+    const int64_t hist = 256 * ntiles;
+    return align256(sizeof(int) * size_t(hist)) + scan_workspace_bytes(hist);
+}
+
+cudaError_t sort_pass8(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out, uint32_t* vals_out,
+                       int64_t n, void* ws, size_t ws_bytes, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    if (ws_bytes < sort_pass8_workspace_bytes(n)) return cudaErrorInvalidValue;
+    const int64_t ntiles = (n + kTile - 1) / kTile;
+    const int64_t hist_n = 256 * ntiles;
+    int* hist = static_cast<int*>(ws);
+    void* scan_ws = static_cast<char*>(ws) + align256(sizeof(int) * size_t(hist_n));
+    k_digit_hist<<<unsigned(ntiles), kSortThreads, 0, s>>>(keys_in, n, 0, int(ntiles), hist);
+    cudaError_t e = exclusive_scan(hist, hist_n, scan_ws, s);
+    if (e != cudaSuccess) return e;
+    k_digit_scatter<<<unsigned(ntiles), kSortThreads, 0, s>>>(keys_in, vals_in, n, 0, int(ntiles), hist, keys_out,
+                                                             vals_out);
+    return cudaGetLastError();
+}
+
 cudaError_t sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out, uint32_t* vals_out,
                        int64_t n, int key_bits, void* ws, size_t ws_bytes, cudaStream_t s) {
     if (n <= 0) return cudaSuccess;

@@ -23,4 +23,10 @@ size_t sort_workspace_bytes(int64_t n);
 cudaError_t sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out, uint32_t* vals_out,
                        int64_t n, int key_bits, void* ws, size_t ws_bytes, cudaStream_t s);
 
+// One stable pass over 8-bit keys (key < 256): the same pass as sort_pairs
+// with key_bits = 8, without its ping-pong buffers.  Scratch bytes:
+size_t sort_pass8_workspace_bytes(int64_t n);
+cudaError_t sort_pass8(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out, uint32_t* vals_out,
+                       int64_t n, void* ws, size_t ws_bytes, cudaStream_t s);
+
 }  // namespace tk

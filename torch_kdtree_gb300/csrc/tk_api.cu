@@ -54,10 +54,16 @@ void clear_error() { g_err.clear(); }
 
 // ------------------------------------------------------------ binning --
 
-__global__ void k_bin_scatter(int nq, const int* bin_of, const int* pos_of, const int* offsets, int* order) {
+// Queries in cell order; with `classes`, each one's cost class (bits 16-23
+// of bin_of, see k_bin_count) goes to the same position.
+__global__ void k_bin_scatter(int nq, const int* bin_of, const int* pos_of, const int* offsets, int* order,
+                              uint32_t* classes) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nq) return;
-    order[offsets[bin_of[i]] + pos_of[i]] = i;
+    const int b = bin_of[i];
+    const int dst = offsets[b & 0xFFFF] + pos_of[i];
+    order[dst] = i;
+    if (classes) classes[dst] = uint32_t(b) >> 16;
 }
 
 // ------------------------------------------------------------ planning --
@@ -70,8 +76,12 @@ int bin_levels(int L, int64_t nq) {
     return std::max(1, std::min({L, kMaxBinLevels, lg - 4}));
 }
 
+// Query workspace: work counter, cell counts, per query its cell, rank,
+// place in cell order and cost class, then the scratch of the cell-count
+// scan or (used after it) of the cost-class pass.  After the cell scatter
+// bin_of and pos_of are free again and receive the class pass's output.
 struct WsLayout {
-    size_t counter = 0, counts = 0, bin_of = 0, pos_of = 0, order = 0, scan = 0, total = 0;
+    size_t counter = 0, counts = 0, bin_of = 0, pos_of = 0, order = 0, classes = 0, scan = 0, total = 0;
 };
 
 WsLayout ws_layout(int L, int64_t nq) {
@@ -88,8 +98,10 @@ WsLayout ws_layout(int L, int64_t nq) {
     o += align_up(sizeof(int) * size_t(nq), 256);
     w.order = o;
     o += align_up(sizeof(int) * size_t(nq), 256);
+    w.classes = o;
+    o += align_up(sizeof(uint32_t) * size_t(nq), 256);
     w.scan = o;
-    o += scan_workspace_bytes(int64_t(1) << B);
+    o += std::max(scan_workspace_bytes(int64_t(1) << B), sort_pass8_workspace_bytes(nq));
     w.total = o;
     return w;
 }
@@ -137,10 +149,15 @@ int pow2_ceil(int v) {
 
 // Zero the work counter and, when binning is on, order the queries by the
 // tree cell at depth B they fall into (count, exclusive scan, scatter).
-// `count(B, counts, bin_of, pos_of)` launches the counting kernel.
+// `count(B, counts, bin_of, pos_of)` launches the counting kernel.  With
+// `classes` (the counting kernel wrote cost classes), one stable radix pass
+// then puts the costliest class first, cell order kept within a class: the
+// persistent search takes its work in that order, so the expensive queries
+// do not end up in the last chunks (the launch's tail), and a warp's 32
+// queries have similar costs (a warp runs as long as its slowest lane).
 template <typename CountFn>
 int prepare_order(const tk_tree* t, int nq, const tk_query_opts& o, char* ws, cudaStream_t s, int** counter,
-                  const int32_t** order, CountFn count) {
+                  const int32_t** order, bool classes, CountFn count) {
     const int L = t->levels;
     const WsLayout w = ws_layout(L, nq);
     *counter = reinterpret_cast<int*>(ws + w.counter);
@@ -167,10 +184,18 @@ int prepare_order(const tk_tree* t, int nq, const tk_query_opts& o, char* ws, cu
         count(B, counts, bin_of, pos_of);
         e = exclusive_scan(counts, nbins, ws + w.scan, s);
         if (e != cudaSuccess) return fail(TK_ECUDA, std::string("bin scan: ") + cudaGetErrorString(e));
-        k_bin_scatter<<<(nq + 255) / 256, 256, 0, s>>>(nq, bin_of, pos_of, counts, ord);
+        uint32_t* cls = classes ? reinterpret_cast<uint32_t*>(ws + w.classes) : nullptr;
+        k_bin_scatter<<<(nq + 255) / 256, 256, 0, s>>>(nq, bin_of, pos_of, counts, ord, cls);
         e = cudaGetLastError();
         if (e != cudaSuccess) return fail(TK_ECUDA, std::string("binning launch: ") + cudaGetErrorString(e));
         *order = ord;
+        if (classes) {
+            uint32_t* final_order = reinterpret_cast<uint32_t*>(pos_of);
+            e = sort_pass8(cls, reinterpret_cast<const uint32_t*>(ord), reinterpret_cast<uint32_t*>(bin_of),
+                           final_order, nq, ws + w.scan, w.total - w.scan, s);
+            if (e != cudaSuccess) return fail(TK_ECUDA, std::string("cost-class pass: ") + cudaGetErrorString(e));
+            *order = reinterpret_cast<const int32_t*>(final_order);
+        }
     } else {
         e = cudaMemsetAsync(*counter, 0, sizeof(int), s);
         if (e != cudaSuccess) return fail(TK_ECUDA, std::string("memset: ") + cudaGetErrorString(e));
@@ -223,8 +248,9 @@ int run_query(const tk_tree* t, const T* q, int nq, int k, T* dists, int32_t* id
 
     int* counter = nullptr;
     const int32_t* order = nullptr;
-    int rc0 = prepare_order(t, nq, o, ws, s, &counter, &order, [&](int B, int* counts, int* bin_of, int* pos_of) {
-        bin_count_launch<T, D>(q, nq, static_cast<const T*>(t->d_medians), B, counts, bin_of, pos_of, s);
+    const PointRec<T>* boxes = static_cast<const PointRec<T>*>(t->d_boxes);
+    int rc0 = prepare_order(t, nq, o, ws, s, &counter, &order, true, [&](int B, int* counts, int* bin_of, int* pos_of) {
+        bin_count_launch<T, D>(q, nq, static_cast<const T*>(t->d_medians), B, L, boxes, counts, bin_of, pos_of, s);
     });
     if (rc0 != TK_OK) return rc0;
 
@@ -232,7 +258,7 @@ int run_query(const tk_tree* t, const T* q, int nq, int k, T* dists, int32_t* id
     a.pts = static_cast<const PointRec<T>*>(t->d_pts);
     a.medians = static_cast<const T*>(t->d_medians);
     a.leaf_off = t->d_leaf_off;
-    a.boxes = (o.prune_boxes == 0 && !packet) ? nullptr : static_cast<const PointRec<T>*>(t->d_boxes);
+    a.boxes = static_cast<const PointRec<T>*>(t->d_boxes);  // the 1-3-D searches always prune with node boxes
     a.levels = L;
     a.smem_levels = S;
     a.q = q;
@@ -284,7 +310,7 @@ int run_query_wide(const tk_tree* t, const T* q, int nq, int k, T* dists, int32_
 
     int* counter = nullptr;
     const int32_t* order = nullptr;
-    const int rc0 = prepare_order(t, nq, o, ws, s, &counter, &order, [&](int B, int* counts, int* bin_of, int* pos_of) {
+    const int rc0 = prepare_order(t, nq, o, ws, s, &counter, &order, false, [&](int B, int* counts, int* bin_of, int* pos_of) {
         bin_count_wide_launch<T>(q, nq, t->dims, static_cast<const T*>(t->d_medians), B, counts, bin_of, pos_of, s);
     });
     if (rc0 != TK_OK) return rc0;
@@ -737,15 +763,18 @@ int tk_tree_query(const tk_tree* t, const void* q, int64_t nq, int k, void* dist
 // ------------------------------------------------ allocation-free query --
 //
 // Scratch of tk_tree_query_noalloc: one static device array, sized for
-// TK_NOALLOC_MAX_QUERIES queries (counter + 2^16 cell counts + three int32
-// arrays of that many queries + the cell-count scan's tile sums, laid out as
-// ws_layout() lays out a caller's workspace).  Every GPU that loads the library holds it until the process
-// exits, and every call on a device shares it.
+// TK_NOALLOC_MAX_QUERIES queries (counter + 2^16 cell counts + four 32-bit
+// arrays of that many queries + the scratch of the cost-class radix pass:
+// 256 counts per tile of 2,048 queries and their scan's tile sums, laid out
+// as ws_layout() lays out a caller's workspace; the call checks the layout
+// against this size before any launch).  Every GPU that loads the library
+// holds it until the process exits, and every call on a device shares it.
 namespace tk {
 namespace {
 
-constexpr size_t kNoAllocScratchBytes =
-    256 + sizeof(int) * (size_t(1) << kMaxBinLevels) + 3 * sizeof(int) * size_t(TK_NOALLOC_MAX_QUERIES) + 256;
+constexpr size_t kNoAllocScratchBytes = 256 + sizeof(int) * (size_t(1) << kMaxBinLevels) +
+                                        4 * sizeof(int) * size_t(TK_NOALLOC_MAX_QUERIES) +
+                                        sizeof(int) * 256 * ((size_t(TK_NOALLOC_MAX_QUERIES) + 2047) / 2048) + 1024;
 static_assert(TK_NOALLOC_MAX_QUERIES % 64 == 0, "each scratch array must stay 256-byte aligned");
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
