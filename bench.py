@@ -128,29 +128,41 @@ def fp64_error(ref, q, dists, idx, chunk=1 << 18):
     return {"max_rel_err": worst, "queries_with_equal_distances_in_list": ties}
 
 
-def profiled_value(kernel_tag: str, field: str = "traffic_bytes_per_launch"):
+def profiled_value(kernel_tag: str, field: str = "traffic_bytes_per_launch", shape: str | None = None):
     """A per-launch figure of a kernel from its committed ncu summary
-    (profiles/<kernel_tag>.md, line '<field>: <int>'), or None."""
+    (profiles/<kernel_tag>.md, line '<field>: <int>'), or None.  With
+    `shape`, only if the summary's 'profiled_shape:' line names that launch
+    shape (a figure of another shape is not this launch's)."""
     path = os.path.join(ROOT, "profiles", kernel_tag + ".md")
     try:
-        m = re.search(field + r":\s*([0-9]+)", open(path).read())
-        return int(m.group(1)) if m else None
+        text = open(path).read()
     except OSError:
         return None
+    if shape is not None:
+        m = re.search(r"profiled_shape:\s*(.+)", text)
+        if not m or m.group(1).strip() != shape:
+            return None
+    m = re.search(field + r":\s*([0-9]+)", text)
+    return int(m.group(1)) if m else None
 
 
-def profiled_traffic(kernel_tag: str):
+def profiled_traffic(kernel_tag: str, shape: str | None = None):
     """DRAM bytes (read + write) per launch from the kernel's ncu summary, or None."""
-    return profiled_value(kernel_tag, "traffic_bytes_per_launch")
+    return profiled_value(kernel_tag, "traffic_bytes_per_launch", shape)
 
 
-def issue_roofline(kernel_tag: str, kernel_ms: float, dev_index: int):
+def launch_shape(levels: int, lanes: int, traversal: int) -> str:
+    """The key a profile summary's 'profiled_shape:' line must carry."""
+    return f"levels={levels} threads_per_query={lanes} traversal={traversal}"
+
+
+def issue_roofline(kernel_tag: str, kernel_ms: float, dev_index: int, shape: str | None = None):
     """Instruction-issue roofline of an issue-bound kernel: warp instructions
-    per launch (from its ncu summary) over the measured launch time, against
-    one warp instruction per cycle per scheduler (4 per SM) at the maximum SM
-    clock."""
+    per launch (from its ncu summary, of the same launch shape) over the
+    measured launch time, against one warp instruction per cycle per
+    scheduler (4 per SM) at the maximum SM clock."""
     import torch
-    inst = profiled_value(kernel_tag, "warp_instructions_per_launch")
+    inst = profiled_value(kernel_tag, "warp_instructions_per_launch", shape)
     if inst is None:
         return None
     props = torch.cuda.get_device_properties(dev_index)
@@ -167,9 +179,16 @@ def issue_roofline(kernel_tag: str, kernel_ms: float, dev_index: int):
 
 
 def algorithmic_bytes(n_ref, nq, k, levels, d=3):
-    """Bytes a KD query launch must move at minimum: queries in (4d per query),
-    results out (8k per query), and the tree once: point records (16 B each),
-    split values (4 B each) and leaf offsets (4 B each)."""
+    """Bytes a KD query launch must move at minimum: queries in (4d per
+    query), results out (8k per query: distance + index), and the tree once:
+    4d bytes per reference point and 8 bytes per split node (the reference's
+    {axis, value} record)."""
+    return nq * (4 * d + 8 * k) + 4 * d * n_ref + 8 * ((1 << levels) - 1)
+
+
+def layout_bytes(n_ref, nq, k, levels, d=3):
+    """The same minimum in this engine's layout: 16-byte point records
+    (coordinates + original index), 4-byte split values and leaf offsets."""
     return nq * (4 * d + 8 * k) + 16 * n_ref + 4 * ((1 << levels) - 1) + 4 * ((1 << levels) + 1)
 
 
@@ -386,7 +405,10 @@ def run_ours(args, rank, world):
     alg = algorithmic_bytes(n_ref, nq, K_NN, ch.levels)
     achieved = alg / (kern_avg / 1e3) / 1e9
     kernel_name = "k_kd_packet" if ch.traversal == 2 else "k_kd_query"
-    traffic = profiled_traffic(kernel_name[2:] + "_cube_sphere_4M_k16")
+    shape = launch_shape(ch.levels, ch.threads_per_query, ch.traversal)
+    prof_tag = kernel_name[2:] + "_cube_sphere_4M_k16"
+    traffic = profiled_traffic(prof_tag, shape)
+    issue = issue_roofline(prof_tag, kern_avg, dev.index, shape)
     fp64 = fp64_error(ref, q, d_ch, i_ch)
 
     # ---- CPU baseline (oracle / reference CPU path) on a bounded sample, plus an exactness check of that sample
@@ -395,6 +417,9 @@ def run_ours(args, rank, world):
     if not args.no_cpu_baseline:
         cpu, exact = cpu_baseline(ref_np, q_np, i_ch[: args.ref_sample].cpu().numpy(),
                                   d_ch[: args.ref_sample].cpu().numpy(), args.ref_sample)
+    rows = None
+    if world == 1 and not args.no_rows:
+        rows = run_rows(args, dev, flush)
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -414,9 +439,18 @@ def run_ours(args, rank, world):
         "identical_results_plain_vs_chosen": same,
         "autotune_table": [list(map(lambda x: round(x, 4) if isinstance(x, float) else x, r)) for r in ch.table],
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_kind": peak_kind, "traffic": traffic, "kernel": kernel_name,
-                     "kernel_ms": kern_avg, "algorithmic_bytes_per_launch": alg,
-                     "issue": issue_roofline(kernel_name[2:] + "_cube_sphere_4M_k16", kern_avg, dev.index)},
+                     "peak_kind": peak_kind, "traffic": traffic, "kernel": kernel_name, "kernel_ms": kern_avg,
+                     "algorithmic_bytes_per_launch": alg,
+                     "algorithmic_bytes_basis": "1,048,576 x (12 B query + 128 B results) + 12 B per reference "
+                                                "point + 8 B per split node",
+                     "layout_bytes_per_launch": layout_bytes(n_ref, nq, K_NN, ch.levels),
+                     "layout_frac": layout_bytes(n_ref, nq, K_NN, ch.levels) / (kern_avg / 1e3) / 1e9 / peak,
+                     "traffic_profile": f"profiles/{prof_tag}.md" if traffic is not None else None,
+                     "profiled_shape": shape if traffic is not None else
+                     f"no committed profile of this launch shape ({shape})",
+                     "binding": "instruction issue (see issue): the search is bound by divergent control flow "
+                                "and L2 latency, not by DRAM bandwidth",
+                     "issue": issue},
         "cpu_baseline": cpu,
         "exactness_vs_oracle_sample": exact,
         "fp32_dists_vs_fp64_recomputation": fp64,
@@ -427,10 +461,12 @@ def run_ours(args, rank, world):
                             "straight into the pinned host buffers",
                 "ms_per_step": t_e2e / args.steps},
         # per chosen step (one graph replay): k_bin_count, the three kernels of the
-        # cell-count scan (k_scan_tiles, k_scan_single, k_scan_add), k_bin_scatter
+        # cell-count scan (k_scan_tiles, k_scan_single, k_scan_add), k_bin_scatter,
+        # the cost-class pass (k_digit_hist, three scan kernels, k_digit_scatter)
         # and the KD query kernel
-        "gpu_launches": 6 * args.steps,
+        "gpu_launches": 11 * args.steps,
         "clocks": clocks,
+        "other_workloads": rows,
     }
     print(json.dumps(line), flush=True)
 
@@ -454,6 +490,263 @@ def cpu_baseline(ref_np, q_np, gpu_idx, gpu_d, sample):
     exact = {"queries": sample, "index_mismatches_non_tie": cmp.mismatches, "tie_queries": cmp.tie_queries,
              "dist_bit_mismatches": cmp.dist_bit_mismatch}
     return cpu, exact
+
+
+# ------------------------------------------- the other workloads' rows --
+#
+# Bounded versions of the other benchmark workloads, run after the headline
+# on the same GPU and reported inside its JSON line: each with its own CUDA
+# event timing, a roofline against its own bound and exactness against the
+# oracle (never against another GPU path).
+
+FP32_NOMINAL_TFLOPS = 152 * 128 * 2 * 2070e6 / 1e12  # CUDA-core FP32 FMA rate at the maximum SM clock
+
+
+def measured_peak_bf16():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["bf16_tflops"]), "measured"
+    except (OSError, ValueError, KeyError):
+        return 1900.0, "fallback"
+
+
+def _median(ms):
+    return float(statistics.median(ms))
+
+
+def _cmp_dict(c):
+    return {"queries": c.n_queries, "index_mismatches_non_tie": c.mismatches, "tie_queries": c.tie_queries,
+            "dist_bit_mismatches": c.dist_bit_mismatch}
+
+
+def row_plain(dev, steps, warmup, threads):
+    """Plain KD query: 100,000 refs and 10,000 queries N(0,1)*1e3, k=5, the
+    reference's default depth; one graph-replayed query vs the oracle's
+    restatement of the reference CPU query on the same inputs."""
+    import torch
+
+    import torch_kdtree_gb300 as tk
+    from oracle import oracle as O
+    from torch_kdtree_gb300.nn_distance import knn_query_raw
+    from torch_kdtree_gb300.synthetic import plain_cloud
+    ref_np, q_np = plain_cloud()
+    ref, q = torch.from_numpy(ref_np).to(dev), torch.from_numpy(q_np).to(dev)
+    k = 5
+    tree = tk.build_kd_tree(ref)
+    d = torch.empty(len(q), k, device=dev)
+    i = torch.empty(len(q), k, dtype=torch.int32, device=dev)
+    s = torch.cuda.Stream(dev)
+    s.wait_stream(torch.cuda.current_stream(dev))
+    with torch.cuda.stream(s):
+        knn_query_raw(tree._tree, q, k, d, i)
+    torch.cuda.current_stream(dev).wait_stream(s)
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        knn_query_raw(tree._tree, q, k, d, i)
+    ms = _median(_event_ms(g.replay, max(steps, 20), warmup))
+    g.replay()
+    torch.cuda.synchronize()
+    lay = O.build_tree(ref_np, O.default_levels(len(ref_np)), nthreads=threads)
+    t0 = time.perf_counter()
+    od, oi = O.query_tree(lay, q_np, k, nthreads=threads)
+    cpu_s = time.perf_counter() - t0
+    alg = algorithmic_bytes(len(ref_np), len(q_np), k, tree.levels)
+    peak, kind = measured_peak_hbm()
+    return {"workload": "100,000 refs x 10,000 queries N(0,1)*1e3, d=3, k=5, levels 13 (reference default), "
+                        "graph-replayed", "value": len(q_np) / (ms / 1e3), "unit": UNIT, "ms_per_step": ms,
+            "roofline": {"bound": "hbm", "achieved": alg / (ms / 1e3) / 1e9, "peak": peak, "peak_kind": kind,
+                         "unit": "GB/s", "frac": alg / (ms / 1e3) / 1e9 / peak, "algorithmic_bytes_per_launch": alg,
+                         "binding": "launch and latency: 10,000 queries are a fraction of one wave"},
+            "cpu_baseline": {"value": len(q_np) / cpu_s, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": "all 10,000 queries"},
+            "exactness_vs_oracle": _cmp_dict(O.compare_knn(od, oi, d.cpu().numpy(), i.cpu().numpy()))}
+
+
+def row_backward(dev, steps, warmup, flush, threads):
+    """Differentiable KNN: 1,048,576 refs and queries N(0,1), k=8, loss =
+    0.5 * sum(dists * w): forward query vs the hand-written backward, the
+    gradient against the reference's torch-indexed formula and against FP64
+    central differences (step 1e-4) on the first 4,096 queries, the forward
+    against the oracle on a query sample."""
+    import torch
+
+    import torch_kdtree_gb300 as tk
+    from oracle import oracle as O
+    from torch_kdtree_gb300._lib import QueryOpts
+    from torch_kdtree_gb300.autograd import knn_backward
+    from torch_kdtree_gb300.nn_distance import knn_query_raw
+    from torch_kdtree_gb300.synthetic import differentiable
+    ref_np, q_np, w_np = differentiable()
+    ref, q, w = (torch.from_numpy(a).to(dev) for a in (ref_np, q_np, w_np))
+    k, n = 8, len(ref_np)
+    tree = tk.build_kd_tree(ref, levels=16, query_opts=QueryOpts.make(threads_per_query=1))
+    d = torch.empty(n, k, device=dev)
+    i = torch.empty(n, k, dtype=torch.int32, device=dev)
+    fwd = _median(_event_ms(lambda: knn_query_raw(tree._tree, q, k, d, i, tree.query_opts), steps, warmup, flush))
+    g = 0.5 * w
+    bwd = _median(_event_ms(lambda: knn_backward(q, ref, i, g, True, True), steps, warmup, flush))
+    gq, gr = knn_backward(q, ref, i, g, True, True)
+    # the reference's gradient: torch autograd through dists re-gathered by index (nn_distance.py:111-112)
+    qq, rr = q.clone().requires_grad_(True), ref.clone().requires_grad_(True)
+    dd = ((qq[:, None, :] - rr[i.long()]) ** 2).sum(-1)
+    tq, tr = torch.autograd.grad((dd * g).sum(), (qq, rr))
+    rel = lambda a, b: float((a - b).abs().max() / b.abs().max().clamp_min(1e-30))
+    # FP64 central differences of the loss on the first 4,096 queries: each
+    # perturbed copy is searched again by an FP64 tree (neighbours re-selected)
+    m, h = 4096, 1e-4
+    t64 = tk.build_kd_tree(ref.double())
+    q64 = q[:m].double()
+    pert = q64[None].repeat(6, 1, 1)
+    for c in range(3):
+        pert[2 * c, :, c] += h
+        pert[2 * c + 1, :, c] -= h
+    dp, _ = t64.query(pert.reshape(-1, 3), nr_nns_searches=k)
+    lp = (dp.reshape(6, m, k) * g[:m].double()).sum(-1)
+    fd = torch.stack([(lp[2 * c] - lp[2 * c + 1]) / (2 * h) for c in range(3)], 1)
+    err = (gq[:m].double() - fd).abs()
+    fd_rel = float((err / fd.abs().clamp_min(1e-3)).max())
+    fd_norm = float(err.max() / fd.abs().max())
+    # forward exactness on a sample
+    sample = 65536
+    lay = O.build_tree(ref_np, O.default_levels(n), nthreads=threads)
+    od, oi = O.query_tree(lay, q_np[:sample], k, nthreads=threads)
+    cmp = O.compare_knn(od, oi, d[:sample].cpu().numpy(), i[:sample].cpu().numpy())
+    alg = n * k * (4 + 4 + 12) + n * 24 + n * 12
+    peak, kind = measured_peak_hbm()
+    return {"workload": "1,048,576 refs + 1,048,576 queries N(0,1), d=3, k=8, loss 0.5*sum(dists*w), w U(0,1); "
+                        "levels 16, one lane per query", "forward_ms": fwd, "backward_ms": bwd,
+            "value": bwd / fwd, "unit": "backward / forward time", "target": "< 1.5",
+            "roofline": {"bound": "hbm", "kernel": "backward (all its kernels)", "achieved": alg / (bwd / 1e3) / 1e9,
+                         "peak": peak, "peak_kind": kind, "unit": "GB/s", "frac": alg / (bwd / 1e3) / 1e9 / peak,
+                         "algorithmic_bytes_per_launch": alg,
+                         "algorithmic_bytes_basis": "Q k (4 idx + 4 grad + 12 gather) + Q 24 (q in, dq out) + "
+                                                    "N 12 (dref out)"},
+            "gradient_vs_torch_indexed": {"grad_q_max_rel": rel(gq, tq), "grad_ref_max_rel": rel(gr, tr)},
+            "grad_q_vs_fp64_central_differences": {"queries": m, "step": h, "max_rel_err": fd_rel,
+                                                   "max_err_over_max_grad": fd_norm, "tolerance": 1e-3,
+                                                   "rel_err_floor": "denominator at least 1e-3"},
+            "forward_exactness_vs_oracle": _cmp_dict(cmp)}
+
+
+def row_batched(dev, steps, warmup, flush, threads):
+    """256 ragged clouds (sizes log-uniform in [1e3, 2e5], 8-Gaussian
+    mixtures, queries = half the size, k from {1, 4, 16}): one graph-captured
+    persistent launch vs one launch per cloud; 16 clouds checked against the
+    oracle (the largest, the smallest and spread sizes, every k)."""
+    import torch
+
+    from oracle import oracle as O
+    from torch_kdtree_gb300.batched import BatchedKDTrees
+    from torch_kdtree_gb300.synthetic import ragged_clouds
+    clouds = ragged_clouds(n_clouds=256, seed=0)
+    refs = [torch.from_numpy(r).to(dev) for r, _, _ in clouds]
+    qs = [torch.from_numpy(q).to(dev) for _, q, _ in clouds]
+    ks = [k for _, _, k in clouds]
+    qc = [len(q) for q in qs]
+    q_flat = torch.cat(qs).contiguous()
+    total_q = len(q_flat)
+    tuned_levels = [int(max(1, min(24, round(np.log2(max(2, len(r)) / 16))))) for r, _, _ in clouds]
+    plain = BatchedKDTrees(refs, ks, qc)  # the reference's depth per cloud
+    tuned = BatchedKDTrees(refs, ks, qc, levels=tuned_levels)
+    ms_plain = sum(_event_ms(lambda: plain.query_each(qs), steps, warmup, flush)) / steps
+    replay = tuned.graph(q_flat)
+    ms_batch = sum(_event_ms(replay, steps, warmup, flush)) / steps
+    plain.query_each(qs)
+    replay()
+    torch.cuda.synchronize()
+    same = bool(torch.equal(plain.out_dists, tuned.out_dists) and torch.equal(plain.out_idx, tuned.out_idx))
+    sizes = np.array([len(r) for r, _, _ in clouds])
+    by_size = np.argsort(sizes)
+    pick = {int(by_size[0]), int(by_size[-1])}
+    for kk in (1, 4, 16):
+        cand = [c for c in by_size[::-1] if ks[c] == kk]
+        pick.update(int(c) for c in cand[:: max(1, len(cand) // 4)][:4])
+    for c in by_size[:: max(1, len(by_size) // 16)]:
+        if len(pick) >= 16:
+            break
+        pick.add(int(c))
+    checks = []
+    d_split, i_split = tuned.split(tuned.out_dists), tuned.split(tuned.out_idx)
+    for c in sorted(pick):
+        r_np, q_np, kk = clouds[c]
+        lay = O.build_tree(r_np, O.default_levels(len(r_np)), nthreads=threads)
+        od, oi = O.query_tree(lay, q_np, kk, nthreads=threads)
+        checks.append(O.compare_knn(od, oi, d_split[c].cpu().numpy(), i_split[c].cpu().numpy()))
+    alg = sum(q * (12 + 8 * k) + 12 * len(r) + 8 * ((1 << L) - 1)
+              for (r, _, _), q, k, L in zip(clouds, qc, ks, tuned_levels))
+    peak, kind = measured_peak_hbm()
+    return {"workload": f"256 clouds, {int(sizes.sum())} refs, {total_q} queries, k in {{1,4,16}}, d=3; tuned "
+                        "depth (~16 points per leaf)",
+            "value": total_q / (ms_batch / 1e3), "unit": UNIT, "ms_per_step": ms_batch,
+            "plain_256_launches": {"value": total_q / (ms_plain / 1e3), "ms_per_step": ms_plain},
+            "batched_vs_plain": ms_plain / ms_batch, "identical_results_batched_vs_plain": same,
+            "roofline": {"bound": "hbm", "achieved": alg / (ms_batch / 1e3) / 1e9, "peak": peak, "peak_kind": kind,
+                         "unit": "GB/s", "frac": alg / (ms_batch / 1e3) / 1e9 / peak,
+                         "algorithmic_bytes_per_launch": alg},
+            "exactness_vs_oracle": {"clouds": len(pick), "queries": int(sum(c.n_queries for c in checks)),
+                                    "index_mismatches_non_tie": int(sum(c.mismatches for c in checks)),
+                                    "tie_queries": int(sum(c.tie_queries for c in checks)),
+                                    "dist_bit_mismatches": int(sum(c.dist_bit_mismatch for c in checks))}}
+
+
+def row_brute_tc(dev, steps, warmup, threads):
+    """Tensor-core brute force: 262,144 refs, 65,536 queries N(0,1) in d = 8
+    and 32 with 5% exact duplicate refs, k=32; FP32 CUDA cores vs TF32 and
+    BF16 hi/lo products (over-fetch 2k, exact re-rank); every mode checked
+    against the oracle's exhaustive search on the first 1,024 queries."""
+    import torch
+
+    from oracle import oracle as O
+    from torch_kdtree_gb300.nn_distance import nn_distance_raw
+    from torch_kdtree_gb300.synthetic import tensor_core_brute
+    k, sample = 32, 1024
+    bf16, bkind = measured_peak_bf16()
+    peaks = {"exact": (FP32_NOMINAL_TFLOPS, "nominal FP32 CUDA-core rate at the maximum clock"),
+             "tf32": (bf16 / 2, f"half the {bkind} dense BF16 rate (TF32 runs at half the BF16 rate)"),
+             "bf16_split": (bf16, f"{bkind} dense BF16 rate")}
+    out = {}
+    for dim in (8, 32):
+        ref_np, q_np = tensor_core_brute(d=dim)
+        ref, q = torch.from_numpy(ref_np).to(dev), torch.from_numpy(q_np).to(dev)
+        od, oi = O.brute(ref_np, q_np[:sample], k, nthreads=threads)
+        pairs = len(ref_np) * len(q_np)
+        res = {}
+        for mode in ("exact", "tf32", "bf16_split"):
+            dd = torch.empty(len(q), k, device=dev)
+            ii = torch.empty(len(q), k, dtype=torch.int32, device=dev)
+            ms = _median(_event_ms(lambda: nn_distance_raw(ref, q, k, dd, ii, mode), steps, warmup))
+            tf = 2 * dim * pairs / (ms / 1e3) / 1e12
+            pk, pkind = peaks[mode]
+            res[mode] = {"ms": ms, "pairs_per_s": pairs / (ms / 1e3),
+                         "roofline": {"bound": "tensor" if mode != "exact" else "fp32", "achieved": tf, "peak": pk,
+                                      "peak_kind": pkind, "unit": "TFLOP/s", "frac": tf / pk,
+                                      "basis": "2d flops per (query, reference) pair; selection and re-rank "
+                                               "not counted"},
+                         "exactness_vs_oracle": _cmp_dict(O.compare_knn(od, oi, dd[:sample].cpu().numpy(),
+                                                                        ii[:sample].cpu().numpy()))}
+            if mode != "exact":
+                res[mode]["speedup_vs_exact"] = res["exact"]["ms"] / ms
+        out[f"d{dim}"] = res
+        del ref, q
+    best = min(out["d32"]["tf32"]["ms"], out["d32"]["bf16_split"]["ms"])
+    return {"workload": "262,144 refs x 65,536 queries N(0,1), 5% duplicate refs, k=32, d in {8, 32}",
+            "value": out["d32"]["exact"]["ms"] / best, "unit": "x (tensor-core over FP32 brute force, d=32)",
+            "runs": out}
+
+
+def run_rows(args, dev, flush):
+    """The other workloads' rows, each bounded to a few seconds."""
+    threads = os.cpu_count() or 1
+    steps, warmup = max(3, min(args.steps, 5)), 2
+    rows = {}
+    for name, fn in (("plain_c1", lambda: row_plain(dev, steps, warmup, threads)),
+                     ("backward_c3", lambda: row_backward(dev, steps, warmup, flush, threads)),
+                     ("batched_c4", lambda: row_batched(dev, steps, warmup, flush, threads)),
+                     ("brute_tc_c5", lambda: row_brute_tc(dev, steps, warmup, threads))):
+        t0 = time.perf_counter()
+        rows[name] = fn()
+        rows[name]["wall_s"] = time.perf_counter() - t0
+    return rows
 
 # ------------------------------------------------------ other workloads --
 
@@ -834,6 +1127,7 @@ def main():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--ref-sample", type=int, default=131072)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-rows", action="store_true", help="skip the other workloads' rows after the headline")
     p.add_argument("--levels", type=int, default=0, help="chosen tree depth (skips the autotuner with --tpq)")
     p.add_argument("--tpq", type=int, default=0, help="chosen lanes per query (skips the autotuner with --levels)")
     p.add_argument("--boxes", type=int, default=1, help="chosen: prune with node bounding boxes (with --levels/--tpq)")

@@ -123,7 +123,8 @@ int tk_tree_get_splits(const tk_tree* tree, void* medians, int32_t* leaf_offsets
 typedef struct tk_query_opts {
     int32_t threads_per_query; /* 0 = auto, else 1, 2, 4, 8, 16 or 32 lanes per query */
     int32_t bin_queries;       /* -1 = auto (on from one wave of queries, SMs x 1024), 0 = off,
-                                  1 = reorder queries by tree cell */
+                                  1 = on: queries ordered by tree cell (1-3-D trees: costliest
+                                  cost class first, cell order within a class) */
     int32_t smem_levels;       /* -1 = auto, else top split levels staged in shared memory */
     int32_t block_threads;     /* reserved, 0 (the KD kernel runs 256-thread blocks) */
     int32_t blocks_per_sm;     /* 0 = as many as fit */

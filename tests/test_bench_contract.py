@@ -26,10 +26,26 @@ def test_roofline_inputs_come_from_the_committed_profile():
 
 def test_algorithmic_bytes_of_the_headline_launch():
     b = bench()
-    # 1,048,576 queries x (12 B in + 128 B out) + 4,194,304 records x 16 B + tree arrays at depth 18
+    # 1,048,576 queries x (12 B in + 128 B out) + 4,194,304 points x 12 B + 8 B per split node at depth 18
     got = b.algorithmic_bytes(4_194_304, 1_048_576, 16, 18)
-    assert got == 1_048_576 * 140 + 4_194_304 * 16 + 4 * ((1 << 18) - 1) + 4 * ((1 << 18) + 1)
-    assert 215e6 < got < 217e6
+    assert got == 1_048_576 * 140 + 4_194_304 * 12 + 8 * ((1 << 18) - 1)
+    assert 199e6 < got < 200e6
+    # the same in this engine's layout: 16-byte records, 4-byte splits and leaf offsets
+    lay = b.layout_bytes(4_194_304, 1_048_576, 16, 18)
+    assert lay == 1_048_576 * 140 + 4_194_304 * 16 + 4 * ((1 << 18) - 1) + 4 * ((1 << 18) + 1)
+
+
+def test_profile_figures_only_for_the_profiled_launch_shape(tmp_path, monkeypatch):
+    b = bench()
+    prof = tmp_path / "profiles"
+    prof.mkdir()
+    (prof / "kd_query_x.md").write_text("profiled_shape: " + b.launch_shape(18, 1, 1) + "\n"
+                                        "traffic_bytes_per_launch: 123\nwarp_instructions_per_launch: 456\n")
+    monkeypatch.setattr(b, "ROOT", str(tmp_path))
+    assert b.profiled_traffic("kd_query_x", b.launch_shape(18, 1, 1)) == 123
+    assert b.profiled_traffic("kd_query_x", b.launch_shape(17, 1, 1)) is None
+    assert b.profiled_value("kd_query_x", "warp_instructions_per_launch", b.launch_shape(18, 1, 1)) == 456
+    assert b.profiled_traffic("kd_query_x") == 123
 
 
 def test_every_profile_names_its_command():

@@ -44,6 +44,26 @@ __device__ __forceinline__ uint32_t rec_index(const PointRec<double>& r) {
     return uint32_t(__double_as_longlong(r.w));
 }
 
+// 32-byte (256-bit) stores to global memory; p must be 32-byte aligned.  A
+// lane that writes its own result row stores it in whole 32-byte sectors:
+// rows written into host memory over the CPU link move at ~140 GB/s this
+// way against ~40 GB/s as 16-byte pieces (measured on GB300).
+__device__ __forceinline__ void st_v8(float* p, float a, float b, float c, float d, float e, float f, float g,
+                                      float h) {
+    asm volatile("st.global.v8.f32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"l"(p), "f"(a), "f"(b), "f"(c),
+                 "f"(d), "f"(e), "f"(f), "f"(g), "f"(h)
+                 : "memory");
+}
+__device__ __forceinline__ void st_v8(int32_t* p, int32_t a, int32_t b, int32_t c, int32_t d, int32_t e,
+                                      int32_t f, int32_t g, int32_t h) {
+    asm volatile("st.global.v8.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"l"(p), "r"(a), "r"(b), "r"(c),
+                 "r"(d), "r"(e), "r"(f), "r"(g), "r"(h)
+                 : "memory");
+}
+__device__ __forceinline__ void st_v4(double* p, double a, double b, double c, double d) {
+    asm volatile("st.global.v4.f64 [%0], {%1, %2, %3, %4};" ::"l"(p), "d"(a), "d"(b), "d"(c), "d"(d) : "memory");
+}
+
 template <typename T, int D>
 __device__ __forceinline__ T sqdist(const T (&q)[D], const PointRec<T>& p) {
     const T d0 = sub_rn(q[0], p.x);
@@ -210,6 +230,28 @@ struct TopK {
 
     // Write the k live slots of this lane to row `row` of the outputs.
     __device__ __forceinline__ void store(int k, int gl, T* out_d, int32_t* out_i, long long row) const {
+        if constexpr (G == 1 && R % 8 == 0) {
+            // all R slots live and both rows 32-byte aligned: whole-sector stores
+            T* pd = out_d + row * k;
+            int32_t* pi = out_i + row * k;
+            if (k == R && ((reinterpret_cast<uintptr_t>(pd) | reinterpret_cast<uintptr_t>(pi)) & 31) == 0) {
+#pragma unroll
+                for (int r = 0; r < R; r += 8) {
+                    if constexpr (sizeof(T) == 4) {
+                        st_v8(pd + r, slot[r].dist(), slot[r + 1].dist(), slot[r + 2].dist(), slot[r + 3].dist(),
+                              slot[r + 4].dist(), slot[r + 5].dist(), slot[r + 6].dist(), slot[r + 7].dist());
+                    } else {
+                        st_v4(pd + r, slot[r].dist(), slot[r + 1].dist(), slot[r + 2].dist(), slot[r + 3].dist());
+                        st_v4(pd + r + 4, slot[r + 4].dist(), slot[r + 5].dist(), slot[r + 6].dist(),
+                              slot[r + 7].dist());
+                    }
+                    st_v8(pi + r, int32_t(slot[r].index()), int32_t(slot[r + 1].index()),
+                          int32_t(slot[r + 2].index()), int32_t(slot[r + 3].index()), int32_t(slot[r + 4].index()),
+                          int32_t(slot[r + 5].index()), int32_t(slot[r + 6].index()), int32_t(slot[r + 7].index()));
+                }
+                return;
+            }
+        }
         if constexpr (G == 1 && R % 4 == 0) {
             // all R slots live and both rows 16-byte aligned: 16-byte stores
             T* pd = out_d + row * k;
