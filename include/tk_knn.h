@@ -173,6 +173,19 @@ int tk_tree_query(const tk_tree* tree, const void* q, int64_t nq, int k, void* d
 int tk_tree_query_host(const tk_tree* tree, const void* q, int64_t nq, int k, void* dists, int32_t* idx,
                        const tk_query_opts* opts, int transfer, void* stream);
 
+/* Exact KNN computed on the host, for a tree built on the host
+ * (tk_tree_create, any device ordinal including -1; a tree built with
+ * tk_tree_create_device keeps no host layout: TK_EINVAL).  q host
+ * [nq, dims], dists host [nq, k], idx host int32 [nq, k]: the same results,
+ * bit for bit, as tk_tree_query of the same tree (reference distance
+ * arithmetic, original indices, lower index among equal distances).  Any
+ * 1 <= k <= n.  n_threads: host threads (0 = all hardware threads).
+ * Blocking; no CUDA call.  Replaces the query of the pybind class
+ * KDTreeCPU<dims>[F] (src/interface.cpp:60-86 -> KDTreeKNNSearch,
+ * src/kdtree.cpp:164-194). */
+int tk_tree_query_cpu(const tk_tree* tree, const void* q, int64_t nq, int k, void* dists, int32_t* idx,
+                      int n_threads);
+
 /* Largest query count tk_tree_query_noalloc accepts in one call. */
 #define TK_NOALLOC_MAX_QUERIES 262144
 

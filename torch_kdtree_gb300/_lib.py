@@ -91,6 +91,7 @@ SIGNATURES = {
     "tk_nn_distance": (_int, [_vp, _i64, _vp, _i64, _int, _int, _int, _int, _vp, _vp, _vp, _sz, _vp]),
     "tk_tree_query_noalloc": (_int, [_vp, _vp, _i64, _int, _vp, _vp, ctypes.POINTER(QueryOpts), _vp]),
     "tk_tree_query_host": (_int, [_vp, _vp, _i64, _int, _vp, _vp, ctypes.POINTER(QueryOpts), _int, _vp]),
+    "tk_tree_query_cpu": (_int, [_vp, _vp, _i64, _int, _vp, _vp, _int]),
     "tk_knn_backward_workspace_size": (_sz, [_i64, _int, _i64]),
     "tk_knn_backward": (_int, [_vp, _vp, _vp, _vp, _i64, _i64, _int, _int, _int, _vp, _vp, _vp, _sz, _vp]),
 }

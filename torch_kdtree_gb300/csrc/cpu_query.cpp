@@ -1,0 +1,174 @@
+// Exact KNN of host queries on a host-built tree ("CPU trees"): the query the
+// reference binds as KDTreeCPU<dims>[F].query (src/interface.cpp:60-86 ->
+// KDTreeKNNSearch, src/kdtree.cpp:164-194), under this engine's contract:
+//  * squared distances with the reference's arithmetic: d_c = q_c - p_c and
+//    ((0 + d0^2) + d1^2) + ... in T, every operation rounded on its own
+//    (this file is compiled without floating-point contraction);
+//  * original point indices, and among equal distances the lower index --
+//    the same answer, bit for bit, as the GPU query of the same tree.
+// The search is depth first from the root: a node is entered only if the
+// bound of its bounding box (per axis the gap from the query to the box,
+// squared and summed like a distance, so by monotonicity of rounding never
+// above the distance of a point inside) does not exceed the current k-th
+// distance; children are taken near side first (the reference's rule,
+// src/kdtree.cpp:30).  Boxes that only tie the k-th distance are still
+// entered, so the result equals an exhaustive search ordered by
+// (distance, original index).  Queries are split into contiguous blocks over
+// host threads.
+#include <algorithm>
+#include <cstdint>
+#include <limits>
+#include <thread>
+#include <vector>
+
+#include "tk_internal.h"
+
+namespace tk {
+namespace {
+
+template <typename T>
+inline bool key_less(T da, uint32_t ia, T db, uint32_t ib) {
+    return da < db || (da == db && ia < ib);  // false whenever da is NaN
+}
+
+template <typename T, int D>
+struct CpuSearch {
+    const HostTree<T>& h;
+    int k;
+    std::vector<T> ld;         // the k best distances, ascending
+    std::vector<uint32_t> li;  // their original indices
+    std::vector<int> stack;
+
+    CpuSearch(const HostTree<T>& tree, int kk) : h(tree), k(kk), ld(kk), li(kk) {
+        stack.reserve(2 * kMaxLevels + 2);
+    }
+
+    T box_bound(int node, const T* q) const {
+        const int S = h.box_stride();
+        const T* lo = h.box_lo.data() + size_t(node) * S;
+        const T* hi = h.box_hi.data() + size_t(node) * S;
+        T b = T(0);
+        for (int c = 0; c < D; ++c) {
+            const T g = q[c] < lo[c] ? T(q[c] - lo[c]) : (q[c] > hi[c] ? T(q[c] - hi[c]) : T(0));
+            const T e = T(g * g);
+            b = c == 0 ? e : T(b + e);
+        }
+        return b;
+    }
+
+    void offer(T d, uint32_t i) {
+        if (!key_less(d, i, ld[k - 1], li[k - 1])) return;
+        int p = k - 1;
+        while (p > 0 && key_less(d, i, ld[p - 1], li[p - 1])) {
+            ld[p] = ld[p - 1];
+            li[p] = li[p - 1];
+            --p;
+        }
+        ld[p] = d;
+        li[p] = i;
+    }
+
+    void run(const T* q, T* out_d, int32_t* out_i) {
+        std::fill(ld.begin(), ld.end(), std::numeric_limits<T>::infinity());
+        std::fill(li.begin(), li.end(), 0xFFFFFFFFu);
+        bool nan_q = false;
+        for (int c = 0; c < D; ++c) nan_q |= q[c] != q[c];
+        if (!nan_q) {  // a query with a NaN coordinate has only NaN distances: nothing enters its list
+            const int L = h.levels;
+            const int first_leaf = (1 << L) - 1;
+            stack.clear();
+            stack.push_back(0);
+            while (!stack.empty()) {
+                const int node = stack.back();
+                stack.pop_back();
+                if (!(box_bound(node, q) <= ld[k - 1])) continue;
+                if (node >= first_leaf) {
+                    const int leaf = node - first_leaf;
+                    const int beg = h.leaf_off[leaf], end = h.leaf_off[leaf + 1];
+                    for (int j = beg; j < end; ++j) {
+                        const T* p = h.structured.data() + size_t(j) * D;
+                        T acc = T(0);
+                        for (int c = 0; c < D; ++c) {
+                            const T dc = T(q[c] - p[c]);
+                            const T sq = T(dc * dc);
+                            acc = c == 0 ? sq : T(acc + sq);
+                        }
+                        offer(acc, uint32_t(h.perm[j]));
+                    }
+                    continue;
+                }
+                const int depth = 31 - __builtin_clz(unsigned(node) + 1u);
+                const int ax = depth % D;
+                const bool left_near = q[ax] < h.medians[node];
+                stack.push_back(2 * node + (left_near ? 2 : 1));  // far child: visited after the near one
+                stack.push_back(2 * node + (left_near ? 1 : 2));
+            }
+        }
+        for (int r = 0; r < k; ++r) {
+            out_d[r] = ld[r];
+            out_i[r] = int32_t(li[r]);
+        }
+    }
+};
+
+template <typename T, int D>
+void search_block(const HostTree<T>& h, const T* q, int64_t b, int64_t e, int k, T* dists, int32_t* idx) {
+    CpuSearch<T, D> s(h, k);
+    for (int64_t i = b; i < e; ++i) s.run(q + i * D, dists + i * k, idx + i * k);
+}
+
+template <typename T, int D>
+void search_all(const HostTree<T>& h, const T* q, int64_t nq, int k, T* dists, int32_t* idx, int n_threads) {
+    int nt = n_threads > 0 ? n_threads : int(std::max(1u, std::thread::hardware_concurrency()));
+    nt = int(std::min<int64_t>(nt, std::max<int64_t>(1, nq / 64)));
+    if (nt <= 1) {
+        search_block<T, D>(h, q, 0, nq, k, dists, idx);
+        return;
+    }
+    std::vector<std::thread> pool;
+    pool.reserve(nt);
+    for (int t = 0; t < nt; ++t) {
+        const int64_t b = nq * t / nt, e = nq * (t + 1) / nt;
+        pool.emplace_back(search_block<T, D>, std::cref(h), q, b, e, k, dists, idx);
+    }
+    for (auto& th : pool) th.join();
+}
+
+template <typename T>
+int query_cpu(const HostTree<T>& h, const T* q, int64_t nq, int k, T* dists, int32_t* idx, int n_threads) {
+    switch (h.dims) {
+        case 1: search_all<T, 1>(h, q, nq, k, dists, idx, n_threads); break;
+        case 2: search_all<T, 2>(h, q, nq, k, dists, idx, n_threads); break;
+        case 3: search_all<T, 3>(h, q, nq, k, dists, idx, n_threads); break;
+        case 4: search_all<T, 4>(h, q, nq, k, dists, idx, n_threads); break;
+        case 5: search_all<T, 5>(h, q, nq, k, dists, idx, n_threads); break;
+        case 6: search_all<T, 6>(h, q, nq, k, dists, idx, n_threads); break;
+        case 7: search_all<T, 7>(h, q, nq, k, dists, idx, n_threads); break;
+        case 8: search_all<T, 8>(h, q, nq, k, dists, idx, n_threads); break;
+        default: return fail(TK_EUNSUPPORTED, "CPU query: dims must be 1..8");
+    }
+    return TK_OK;
+}
+
+}  // namespace
+}  // namespace tk
+
+extern "C" int tk_tree_query_cpu(const tk_tree* t, const void* q, int64_t nq, int k, void* dists, int32_t* idx,
+                                 int n_threads) {
+    using namespace tk;
+    clear_error();
+    if (!t) return fail(TK_EINVAL, "tree is null");
+    if (!t->host_layout)
+        return fail(TK_EINVAL, "tree was built on the GPU and keeps no host layout; build it on the host "
+                               "(tk_tree_create) to query it on the CPU");
+    if (nq < 0 || nq >= (int64_t(1) << 31)) return fail(TK_EINVAL, "number of queries must be in [0, 2^31)");
+    if (k < 1) return fail(TK_EINVAL, "k must be >= 1");
+    if (k > t->n) return fail(TK_EINVAL, "You requested more nearest neighbors than there are in the KD-Tree");
+    if (nq == 0) return TK_OK;
+    if (!q || !dists || !idx) return fail(TK_EINVAL, "null query or output pointer");
+    if (t->dtype == TK_F32)
+        return query_cpu<float>(t->h32, static_cast<const float*>(q), nq, k, static_cast<float*>(dists), idx,
+                                n_threads);
+    return query_cpu<double>(t->h64, static_cast<const double*>(q), nq, k, static_cast<double*>(dists), idx,
+                             n_threads);
+}

@@ -17,7 +17,9 @@ result_idx=None)``.  Differences, all deliberate:
   instead of torch indexing with atomics;
 * ``levels`` may exceed 13 (the reference's limit came from its kernel's
   shared-memory visit tags), up to 24;
-* only CUDA trees: this engine has no CPU query implementation.
+* a tree built with ``device='cpu'`` (the reference's KDTreeCPU classes) is
+  queried on the host by the library's own threaded search
+  (tk_tree_query_cpu), with exactly the GPU query's answers.
 """
 from __future__ import annotations
 
@@ -113,10 +115,8 @@ class TorchKDTree:
     def __init__(self, points_ref: torch.Tensor, device: torch.device, levels: int, squared_distances: bool,
                  query_opts: Optional[QueryOpts] = None, build: str = "auto"):
         """Builds the KD-tree.  See :func:`build_kd_tree`."""
-        if device.type != "cuda":
-            raise RuntimeError(
-                "Could not find the KD-Tree for your specified options: this engine builds CUDA trees only "
-                f"(requested device {device}).")
+        if device.type not in ("cuda", "cpu"):
+            raise RuntimeError(f"Could not find the KD-Tree for your specified options (device {device}).")
         if points_ref.shape[0] >= 2 ** 31:
             raise AssertionError("Only 32 bit signed indexing implemented")
         dtype, dims = points_ref.dtype, points_ref.shape[-1]
@@ -124,11 +124,21 @@ class TorchKDTree:
             raise RuntimeError(
                 "Could not find the KD-Tree for your specified options. This probably means the library was not "
                 f"compiled for the specified dimensionality ({dims}) or precision ({dtype}).")
+        if build not in ("auto", "host", "device"):
+            raise ValueError("build must be 'auto', 'host' or 'device'")
+        if device.type == "cpu":
+            # the reference's KDTreeCPU<dims>[F]: built and queried on the host
+            if build == "device":
+                raise ValueError("a CPU tree is built on the host (build='host' or 'auto')")
+            self._setup(points_ref, device, levels, squared_distances, query_opts)
+            self.use_gpu = False
+            host = np.ascontiguousarray(points_ref.detach().cpu().numpy())
+            self._tree = _Tree(host, self.levels, -1)
+            self.built_on = "host"
+            return
         if device.index is None:
             device = torch.device("cuda", torch.cuda.current_device())
         self._setup(points_ref, device, levels, squared_distances, query_opts)
-        if build not in ("auto", "host", "device"):
-            raise ValueError("build must be 'auto', 'host' or 'device'")
         if build == "auto":
             build = "device" if points_ref.is_cuda else "host"
         if build == "device":
@@ -209,6 +219,8 @@ class TorchKDTree:
             raise RuntimeError("You requested more nearest neighbors than there are in the KD-Tree")
         if k < 1:
             raise RuntimeError("nr_nns_searches must be at least 1")
+        if not self.use_gpu:
+            return self._query_cpu(points_query, k, result_dists, result_idx)
         if k > MAX_K:
             raise RuntimeError(f"nr_nns_searches is limited to {MAX_K} on the GPU")
         host_out = (result_dists is not None and result_idx is not None and result_dists.device.type == "cpu"
@@ -268,6 +280,35 @@ class TorchKDTree:
         if points_query.dim() != 2 or points_query.shape[1] != self.dims:
             raise AssertionError(f"points_query must be [Q, {self.dims}]")
 
+    def _query_cpu(self, points_query: torch.Tensor, k: int, result_dists: Optional[torch.Tensor],
+                   result_idx: Optional[torch.Tensor]):
+        """Query of a CPU tree: tk_tree_query_cpu on host memory (the
+        reference's KDTreeCPU query, src/kdtree.cpp:164-194).  With a gradient
+        the distances are re-gathered by torch, as the reference does
+        (torch_kdtree/nn_distance.py:111-112)."""
+        points_query = points_query.to(self.device)
+        nq = points_query.shape[0]
+        if result_dists is None:
+            result_dists = torch.empty((nq, k), dtype=self.dtype)
+        if result_idx is None:
+            result_idx = torch.empty((nq, k), dtype=self.dtype_idx)
+        self._check_query(points_query, k, result_dists, result_idx)
+        if result_dists.device.type != "cpu" or result_idx.device.type != "cpu":
+            raise AssertionError("a CPU tree writes its results into CPU tensors")
+        if not result_dists.is_contiguous():
+            result_dists = result_dists.contiguous()
+        if not result_idx.is_contiguous():
+            result_idx = result_idx.contiguous()
+        q = points_query.detach().contiguous()
+        check(LIB.tk_tree_query_cpu(self._tree.handle, q.data_ptr(), nq, k, result_dists.data_ptr(),
+                                    result_idx.data_ptr(), 0))
+        dists, inds = result_dists, result_idx
+        if (points_query.requires_grad or self.ref_requires_grad) and torch.is_grad_enabled():
+            dists = torch.sum((points_query[:, None] - self.points_ref_bak[inds.long()]) ** 2, dim=-1)
+        if not self.squared_distances:
+            dists = torch.sqrt(dists)
+        return dists, inds
+
     def _query_host(self, points_query: torch.Tensor, k: int, result_dists: torch.Tensor,
                     result_idx: torch.Tensor):
         """CPU queries into CPU result buffers through tk_tree_query_host."""
@@ -289,12 +330,14 @@ def build_kd_tree(points_ref: Union[torch.Tensor, np.ndarray], device: Optional[
                   query_opts: Optional[QueryOpts] = None, build: str = "auto") -> TorchKDTree:
     """Builds the KD-tree for subsequent queries (torch_kdtree/nn_distance.py:119-160).
 
-    The tree has the reference's layout and lives on the GPU.  ``build``:
-    "host" builds it on the CPU (as the reference does) and uploads it once;
-    "device" builds it on the GPU from the CUDA tensor (same layout, no host
-    copy); "auto" (default) picks "device" for CUDA input, else "host".
-    ``device`` defaults to ``points_ref.device`` (which must then be CUDA);
-    ``levels`` defaults to the reference's heuristic and may range 1..24."""
+    The tree has the reference's layout.  On a CUDA ``device`` it lives on
+    the GPU; ``build``: "host" builds it on the CPU (as the reference does)
+    and uploads it once; "device" builds it on the GPU from the CUDA tensor
+    (same layout, no host copy); "auto" (default) picks "device" for CUDA
+    input, else "host".  With ``device='cpu'`` (the reference's KDTreeCPU
+    trees) it is built and queried on the host.  ``device`` defaults to
+    ``points_ref.device``; ``levels`` defaults to the reference's heuristic
+    and may range 1..24."""
     if issubclass(type(points_ref), np.ndarray):
         points_ref = torch.from_numpy(points_ref)
     if device is None:
@@ -333,19 +376,21 @@ def load_kd_tree(path, device: Optional[torch.device] = None, squared_distances:
     if perm.shape != (n,) or med.shape != ((1 << levels) - 1,) or off.shape != ((1 << levels) + 1,):
         raise ValueError("layout arrays have inconsistent shapes")
     device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
-    if device.type != "cuda":
-        raise RuntimeError("this engine builds CUDA trees only")
-    if device.index is None:
+    if device.type not in ("cuda", "cpu"):
+        raise RuntimeError(f"trees live on a CUDA device or on the CPU, not {device}")
+    if device.type == "cuda" and device.index is None:
         device = torch.device("cuda", torch.cuda.current_device())
+    ordinal = device.index if device.type == "cuda" else -1
     h = ctypes.c_void_p()
     check(LIB.tk_tree_create_from_layout(pts.ctypes.data, perm.ctypes.data, med.ctypes.data, off.ctypes.data, n, d,
                                          _lib.TK_F32 if pts.dtype == np.float32 else _lib.TK_F64, levels,
-                                         device.index, ctypes.byref(h)))
+                                         ordinal, ctypes.byref(h)))
     orig = np.empty_like(pts)
     orig[perm] = pts  # the cloud in its original order, for gradients
     tree = TorchKDTree.__new__(TorchKDTree)
     tree._setup(torch.from_numpy(orig).to(device), device, levels, squared_distances, query_opts)
-    tree._tree = _Tree(None, levels, device.index)
+    tree.use_gpu = device.type == "cuda"
+    tree._tree = _Tree(None, levels, ordinal)
     tree._tree.handle = h
     tree.built_on = "file"
     return tree
