@@ -252,6 +252,28 @@ size_t tk_nn_distance_workspace_size(int64_t n, int64_t nq, int dims, int k, int
 int tk_nn_distance(const void* ref, int64_t n, const void* q, int64_t nq, int dims, int k, int dtype, int mode,
                    void* dists, int32_t* idx, void* workspace, size_t workspace_bytes, void* stream);
 
+/* What the last tk_nn_distance call made with `workspace` met on the
+ * device, read back from that workspace after the call has completed
+ * (synchronise its stream first); pass the same shape arguments as that
+ * call.  *flags: bit 0 = a bounded device-side wait of the tensor-core
+ * kernel ran out, bit 1 = an input lay outside the tensor-core
+ * certificate's range; *recomputed = queries the exact kernel recomputed.
+ * The answer is exact in every case: an unfinished or uncertifiable
+ * candidate search only sends its queries to the exact kernel.  Returns
+ * TK_ETIMEOUT when bit 0 is set, else TK_OK; TK_BRUTE_EXACT calls report
+ * zeros.  Replaces the reference's exit() on a device error
+ * (src/cutils.cuh:34-43), which left the caller nothing to inspect. */
+int tk_nn_distance_report(const void* workspace, int64_t n, int64_t nq, int dims, int k, int dtype, int mode,
+                          int* flags, int* recomputed);
+
+/* Poll budget of every bounded device-side wait (the mbarrier waits of the
+ * tensor-core brute force); 0 = the default (2^22 polls, far beyond any
+ * wait that completes).  A small budget makes the waits run out on purpose:
+ * host-side fault injection for tests of the time-out path, whose answers
+ * stay exact (see tk_nn_distance_report).  Process-wide, for later calls;
+ * returns the previous value.  No counterpart in the reference. */
+uint32_t tk_set_device_wait_limit(uint32_t polls);
+
 /* ----------------------------------------------------------- backward -- */
 
 /* Bytes of device scratch tk_knn_backward needs when grad_ref is requested. */

@@ -152,7 +152,7 @@ def test_api_errors():
     with pytest.raises(Exception):
         t.build_kd_tree(np.random.uniform(size=(10, 436)), device="cuda")  # uncompiled dimension
     with pytest.raises(Exception):
-        t.build_kd_tree(torch.randn(10, 3), device="cpu")  # this engine builds CUDA trees only
+        t.build_kd_tree(torch.randn(10, 3), device="meta")  # trees live on a CUDA device or the CPU
     from torch_kdtree_gb300._lib import QueryOpts
     bad = t.build_kd_tree(pts, query_opts=QueryOpts.make(traversal=3))
     with pytest.raises(Exception):

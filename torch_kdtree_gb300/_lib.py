@@ -92,6 +92,9 @@ SIGNATURES = {
     "tk_tree_query_noalloc": (_int, [_vp, _vp, _i64, _int, _vp, _vp, ctypes.POINTER(QueryOpts), _vp]),
     "tk_tree_query_host": (_int, [_vp, _vp, _i64, _int, _vp, _vp, ctypes.POINTER(QueryOpts), _int, _vp]),
     "tk_tree_query_cpu": (_int, [_vp, _vp, _i64, _int, _vp, _vp, _int]),
+    "tk_nn_distance_report": (_int, [_vp, _i64, _i64, _int, _int, _int, _int, ctypes.POINTER(_int),
+                                     ctypes.POINTER(_int)]),
+    "tk_set_device_wait_limit": (ctypes.c_uint32, [ctypes.c_uint32]),
     "tk_knn_backward_workspace_size": (_sz, [_i64, _int, _i64]),
     "tk_knn_backward": (_int, [_vp, _vp, _vp, _vp, _i64, _i64, _int, _int, _int, _vp, _vp, _vp, _sz, _vp]),
 }

@@ -26,6 +26,7 @@
 // brute_tc5_bf16.cu (tcgen05) and brute_tc_mma.cu (mma.sync), compiled in
 // parallel.
 #include <algorithm>
+#include <atomic>
 #include <string>
 
 #include "brute_tc.cuh"
@@ -108,6 +109,10 @@ TcWs tc_layout(int64_t n, int64_t nq, int d, int k, int mode, int sms) {
     return w;
 }
 
+// Poll budget of the candidate kernel's bounded waits (0 = kT5MaxTries); set
+// by tk_set_device_wait_limit.
+std::atomic<uint32_t> g_wait_polls{0};
+
 int sm_count_now() {
     int dev = 0, v = 1;
     cudaGetDevice(&dev);
@@ -165,6 +170,8 @@ int run_brute_tc(const float* ref, int64_t n, const float* q, int64_t nq, int d,
         t5.cand_i = reinterpret_cast<int32_t*>(p + w.cand_i);
         t5.tau = reinterpret_cast<float*>(p + w.tau);
         t5.err = reinterpret_cast<int*>(p + w.err);
+        const uint32_t polls = g_wait_polls.load();
+        t5.max_tries = polls ? polls : kT5MaxTries;
         crc = mode == TK_BRUTE_TF32 ? tc5_dispatch_tf32(t5, w.KP, w.C / 2, qblocks, s)
                                     : tc5_dispatch_bf16(t5, w.KP, w.C / 2, qblocks, s);
         if (crc != TK_OK) return crc;
@@ -239,3 +246,26 @@ int run_brute_tc(const float* ref, int64_t n, const float* q, int64_t nq, int d,
 }
 
 }  // namespace tk
+
+extern "C" uint32_t tk_set_device_wait_limit(uint32_t polls) { return tk::g_wait_polls.exchange(polls); }
+
+extern "C" int tk_nn_distance_report(const void* workspace, int64_t n, int64_t nq, int dims, int k, int dtype,
+                                     int mode, int* flags, int* recomputed) {
+    using namespace tk;
+    using namespace tk::tcx;
+    clear_error();
+    if (!flags || !recomputed) return fail(TK_EINVAL, "null output pointer");
+    *flags = 0;
+    *recomputed = 0;
+    if (mode != TK_BRUTE_TF32 && mode != TK_BRUTE_BF16_SPLIT) return TK_OK;  // the exact kernel has no certificate
+    if (dtype != TK_F32) return fail(TK_EINVAL, "tensor-core modes take float32 inputs");
+    if (!workspace || n < 1 || nq < 1 || k < 1 || dims < 1) return fail(TK_EINVAL, "bad shape or null workspace");
+    const TcWs w = tc_layout(n, nq, dims, k, mode, sm_count_now());
+    const char* p = static_cast<const char*>(workspace);
+    cudaError_t e = cudaMemcpy(flags, p + w.err, sizeof(int), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(recomputed, p + w.fail_count, sizeof(int), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return fail(TK_ECUDA, std::string("report: ") + cudaGetErrorString(e));
+    if (*flags & kTcErrTimeout)
+        return fail(TK_ETIMEOUT, "a bounded device wait ran out; the exact kernel recomputed every query");
+    return TK_OK;
+}

@@ -33,6 +33,10 @@ inline size_t align256(size_t v) { return (v + 255) / 256 * 256; }
 // |r|^2 + 2|q||r| <= 2 (|q|^2 + |r|^2) < 2^127: finite.  Uncertified queries
 // are answered by the exact kernel.
 constexpr float kTcNormLimit = 0x1p125f;
+// Bits of the candidate search's error word (any bit: certify nothing, so
+// the exact kernel recomputes every query and the answer stays exact).
+constexpr int kTcErrTimeout = 1;  // a bounded wait of the tcgen05 kernel ran out
+constexpr int kTcErrRange = 2;    // an input outside the certificate's range (kTcNormLimit)
 
 __device__ __forceinline__ uint32_t to_tf32(float x) {
     uint32_t r;
@@ -61,7 +65,7 @@ __global__ void k_tc_pack(const float* __restrict__ x, int rows, int d, int KP, 
         }
     }
     norm[r] = s;
-    if (err && !(s < kTcNormLimit)) atomicExch(err, 1);  // see kTcNormLimit
+    if (err && !(s < kTcNormLimit)) atomicOr(err, kTcErrRange);  // see kTcNormLimit
 }
 
 struct TcArgs {
@@ -260,7 +264,7 @@ constexpr int kT5BufStride = kT5Buf + 1;  // row stride of the hit buffer (keys)
 constexpr int kT5BatchMin = 8;  // hits of a row merged as one sorted batch from this many on
 constexpr int kT5Threads = 32 * (kT5EpiWarps + 1);
 constexpr float kT5PadNorm = 1e30f;
-constexpr uint32_t kT5MaxTries = 1u << 22;  // bounded mbarrier polls
+constexpr uint32_t kT5MaxTries = 1u << 22;  // bounded mbarrier polls (default; Tc5Args::max_tries)
 
 __device__ __forceinline__ uint32_t core_offset(int row, int kb, int KB) {
     return uint32_t((row >> 3) * (8 * KB) + (kb >> 4) * 128 + (row & 7) * 16 + (kb & 15));
@@ -280,7 +284,7 @@ __global__ void k_tc5_pack(const float* __restrict__ x, int rows, int rows_pad, 
     float nrm = 0.f;
     if (real && !is_query) {
         for (int c = 0; c < d; ++c) nrm = fmaf(x[(long long)r * d + c], x[(long long)r * d + c], nrm);
-        if (!(nrm < kTcNormLimit)) atomicExch(err, 1);  // see kTcNormLimit
+        if (!(nrm < kTcNormLimit)) atomicOr(err, kTcErrRange);  // see kTcNormLimit
     }
     const long long tile_base = (long long)(r / tile_rows) * tile_rows * KB;
     const int rr = r % tile_rows;
@@ -312,7 +316,8 @@ struct Tc5Args {
     float* cand_s;              // [nq, nsplit, 2 * CH]
     int32_t* cand_i;
     float* tau;                 // [nq, nsplit]
-    int* err;                   // set when a bounded wait ran out
+    int* err;                   // kTcErrTimeout set when a bounded wait ran out
+    uint32_t max_tries;         // polls of each mbarrier wait before giving up
 };
 
 // Score keys: order-preserving uint32 image of the float score (negative
@@ -481,6 +486,12 @@ __global__ void __launch_bounds__(kT5Threads, 1) k_tc5_select(const Tc5Args a) {
         // ------------------------------------------------ producer / MMA issuer
         if (lane == 0 && ntiles > 0) {
             bool ok = true;
+            // what this thread started and has not yet seen complete, per
+            // stage: the tile last copied in / waited for, last committed /
+            // waited for (drained if it gives up, see below)
+            bool a_pending = true;
+            int b_issued[2] = {-1, -1}, b_waited[2] = {-1, -1};
+            int m_issued[2] = {-1, -1}, m_waited[2] = {-1, -1};
             sm100::mbar_arrive_expect_tx(&full_a, PL * A_BYTES);
             sm100::bulk_g2s(sA, a.a_hi + (size_t)blockIdx.x * A_BYTES, A_BYTES, &full_a);
             if (PL == 2) sm100::bulk_g2s(sA + A_BYTES, a.a_lo + (size_t)blockIdx.x * A_BYTES, A_BYTES, &full_a);
@@ -490,14 +501,23 @@ __global__ void __launch_bounds__(kT5Threads, 1) k_tc5_select(const Tc5Args a) {
                 if (PL == 2)
                     sm100::bulk_g2s(sB + (t * PL + 1) * B_BYTES, a.b_lo + (size_t)(tile0 + t) * B_BYTES, B_BYTES,
                                     &full_b[t]);
+                b_issued[t] = t;
             }
-            for (int t = 0; t < ntiles && ok; ++t) {
+            for (int t = 0; t < ntiles; ++t) {
                 const int st = t & 1;
-                const uint32_t ph = (t >> 1) & 1;
-                ok = sm100::mbar_wait(&full_b[st], ph, kT5MaxTries);
-                if (ok && t == 0) ok = sm100::mbar_wait(&full_a, 0, kT5MaxTries);
-                if (ok && t >= 2) ok = sm100::mbar_wait(&epi_done[st], ((t - 2) >> 1) & 1, kT5MaxTries);
+                const uint32_t ph = (t >> 1) & 1;  // stage st serves tiles st, st + 2, ...: phase t / 2
+                ok = sm100::mbar_wait(&full_b[st], ph, a.max_tries);
                 if (!ok) break;
+                b_waited[st] = t;
+                if (t == 0) {
+                    ok = sm100::mbar_wait(&full_a, 0, a.max_tries);
+                    if (!ok) break;
+                    a_pending = false;
+                }
+                if (t >= 2) {
+                    ok = sm100::mbar_wait(&epi_done[st], ((t - 2) >> 1) & 1, a.max_tries);
+                    if (!ok) break;
+                }
                 sm100::tc_fence_after();
                 const uint32_t dtm = tmem + uint32_t(st * kT5Cols);
                 const uint32_t a0 = sm100::smem_u32(sA);
@@ -516,20 +536,35 @@ __global__ void __launch_bounds__(kT5Threads, 1) k_tc5_select(const Tc5Args a) {
                     }
                 }
                 sm100::mma_commit(&mma_done[st]);
+                m_issued[st] = t;
                 if (t + 2 < ntiles) {
-                    ok = sm100::mbar_wait(&mma_done[st], ph, kT5MaxTries);  // stage st no longer read
+                    ok = sm100::mbar_wait(&mma_done[st], ph, a.max_tries);  // stage st no longer read
                     if (!ok) break;
+                    m_waited[st] = t;
                     sm100::mbar_arrive_expect_tx(&full_b[st], PL * B_BYTES);
                     sm100::bulk_g2s(sB + (st * PL) * B_BYTES, a.b_hi + (size_t)(tile0 + t + 2) * B_BYTES, B_BYTES,
                                     &full_b[st]);
                     if (PL == 2)
                         sm100::bulk_g2s(sB + (st * PL + 1) * B_BYTES, a.b_lo + (size_t)(tile0 + t + 2) * B_BYTES,
                                         B_BYTES, &full_b[st]);
+                    b_issued[st] = t + 2;
                 }
             }
             if (!ok) {
+                // A wait ran out: flag it (the re-rank then certifies nothing
+                // and the exact kernel answers every query), then let this
+                // thread's own copies and matrix products still in flight
+                // land -- each wait bounded by the default poll count --
+                // before the block frees its tensor memory and exits.
                 atomicExch(&abort_sh, 1);
-                atomicExch(a.err, 1);
+                atomicOr(a.err, kTcErrTimeout);
+                if (a_pending) sm100::mbar_wait(&full_a, 0, kT5MaxTries);
+                for (int s2 = 0; s2 < 2; ++s2) {
+                    if (b_issued[s2] > b_waited[s2])
+                        sm100::mbar_wait(&full_b[s2], (b_issued[s2] >> 1) & 1, kT5MaxTries);
+                    if (m_issued[s2] > m_waited[s2])
+                        sm100::mbar_wait(&mma_done[s2], (m_issued[s2] >> 1) & 1, kT5MaxTries);
+                }
             }
         }
         __syncwarp();
@@ -624,7 +659,7 @@ __global__ void __launch_bounds__(kT5Threads, 1) k_tc5_select(const Tc5Args a) {
             const int base = r0 + t * kT5Cols;
             const uint32_t tcol = trow + uint32_t(st * kT5Cols);
             int w_ok = 1;
-            if (lane == 0) w_ok = sm100::mbar_wait(&mma_done[st], ph, kT5MaxTries);
+            if (lane == 0) w_ok = sm100::mbar_wait(&mma_done[st], ph, a.max_tries);
             w_ok = __shfl_sync(0xFFFFFFFFu, w_ok, 0);
             if (tid == 0) {  // flags of the next tile (their last readers passed this tile's first barrier)
                 sFlag[par ^ 1] = 0;
@@ -671,7 +706,7 @@ __global__ void __launch_bounds__(kT5Threads, 1) k_tc5_select(const Tc5Args a) {
             if (lane == 0) sm100::mbar_arrive(&epi_done[st]);
             bar_epi();
             if (bad) {
-                if (tid == 0) atomicExch(a.err, 1);
+                if (tid == 0) atomicOr(a.err, kTcErrTimeout);
                 break;
             }
         }
