@@ -261,7 +261,6 @@ constexpr int kT5EpiWarps = 16; // 4 per 32-lane quarter of the accumulator when
 constexpr int kT5Chunk = 64;    // accumulator columns per phase (16 per column-group warp)
 constexpr int kT5Buf = 64;      // hit buffer per row: one phase's worth of columns
 constexpr int kT5BufStride = kT5Buf + 1;  // row stride of the hit buffer (keys), spreads rows over banks
-constexpr int kT5BatchMin = 8;  // hits of a row merged as one sorted batch from this many on
 constexpr int kT5Threads = 32 * (kT5EpiWarps + 1);
 constexpr float kT5PadNorm = 1e30f;
 constexpr uint32_t kT5MaxTries = 1u << 22;  // bounded mbarrier polls (default; Tc5Args::max_tries)
@@ -336,87 +335,35 @@ constexpr unsigned long long kScoreSentinel = (0xFF800000ull << 32) | 0xFFFFFFFF
 // A row's over-fetch list of up to 32 * R keys spread over a warp (slot s on
 // lane s % 32, register s / 32; the first 32 R - C slots are padding below
 // every key), as TopK in tk_device.cuh.
-template <int R>
-struct RowList {
-    unsigned long long slot[R];
-    __device__ __forceinline__ void init(int C, int lane) {
+// The over-fetch list of one query row held by a group of 4 lanes: ascending
+// score keys, lane g of the group holding ranks [RS g, RS g + RS) in its
+// registers (RS = C / 4).  An insertion shifts every lane's run in registers
+// and moves one key across each lane boundary with a single shuffle, so the 8
+// groups of a warp insert into their 8 rows side by side.
+template <int RS>
+struct GroupList {
+    unsigned long long slot[RS];
+    __device__ __forceinline__ void init() {
 #pragma unroll
-        for (int r = 0; r < R; ++r) slot[r] = (r * 32 + lane < 32 * R - C) ? 0ull : kScoreSentinel;
+        for (int i = 0; i < RS; ++i) slot[i] = kScoreSentinel;
     }
-    __device__ __forceinline__ void insert(unsigned long long c, int lane) {
-        unsigned long long nw[R];
+    // Insert c (the sentinel leaves the list as it is); every lane of the
+    // warp calls it.  gl: this lane's place in its group.
+    __device__ __forceinline__ void insert(unsigned long long c, int gl) {
+        const unsigned long long before = __shfl_up_sync(0xFFFFFFFFu, slot[RS - 1], 1, 4);
 #pragma unroll
-        for (int r = 0; r < R; ++r) {
-            const unsigned long long old = slot[r];
-            const unsigned long long up = __shfl_up_sync(0xFFFFFFFFu, old, 1);
-            const unsigned long long wrap = r > 0 ? __shfl_sync(0xFFFFFFFFu, slot[r - 1], 31) : 0ull;
-            const unsigned long long prev = lane == 0 ? wrap : up;
-            const bool has_prev = !(lane == 0 && r == 0);
-            nw[r] = old <= c ? old : ((!has_prev || prev <= c) ? c : prev);
+        for (int i = RS - 1; i >= 0; --i) {  // top down: slot[i - 1] is still the old value
+            const unsigned long long old = slot[i];
+            const bool has_prev = i > 0 || gl > 0;
+            const unsigned long long prev = i > 0 ? slot[i - 1] : before;
+            slot[i] = old <= c ? old : ((!has_prev || prev <= c) ? c : prev);
         }
-#pragma unroll
-        for (int r = 0; r < R; ++r) slot[r] = nw[r];
     }
-    __device__ __forceinline__ unsigned long long worst() const { return __shfl_sync(0xFFFFFFFFu, slot[R - 1], 31); }
-
-    // Keep the 32 R smallest of the list and the batch x (32 R keys in the
-    // list's layout, any order, sentinel-padded): bitonic sort of x, then
-    // element-wise min of the list and the reversed batch (which holds the
-    // 32 R smallest of both, as a bitonic sequence) and a bitonic clean-up.
-    // The padding slots at the front are zeros and stay there.
-    __device__ __forceinline__ void merge_batch(unsigned long long (&x)[R], int lane) {
-        constexpr int S = 32 * R;
-#pragma unroll
-        for (int size = 2; size <= S; size <<= 1) {
-#pragma unroll
-            for (int stride = size >> 1; stride > 0; stride >>= 1) {
-                if (stride == 32) {  // partner in the same lane, other register (R == 2)
-#pragma unroll
-                    for (int r = 0; r + 1 < R; r += 2) {
-                        const unsigned long long a = x[r], b = x[r + 1];
-                        x[r] = a < b ? a : b;  // size == 64 == S: ascending
-                        x[r + 1] = a < b ? b : a;
-                    }
-                } else {
-#pragma unroll
-                    for (int r = 0; r < R; ++r) {
-                        const unsigned long long p = __shfl_xor_sync(0xFFFFFFFFu, x[r], stride);
-                        const int sidx = r * 32 + lane;
-                        const bool asc = (sidx & size) == 0;
-                        const bool lower = (lane & stride) == 0;
-                        const bool take_min = asc == lower;
-                        const bool p_less = p < x[r];
-                        x[r] = (take_min == p_less) ? p : x[r];
-                    }
-                }
-            }
-        }
-#pragma unroll
-        for (int r = 0; r < R; ++r) {
-            const unsigned long long b = __shfl_sync(0xFFFFFFFFu, x[R - 1 - r], 31 - lane);
-            slot[r] = b < slot[r] ? b : slot[r];
-        }
-#pragma unroll
-        for (int stride = S >> 1; stride > 0; stride >>= 1) {
-            if (stride == 32) {
-#pragma unroll
-                for (int r = 0; r + 1 < R; r += 2) {
-                    const unsigned long long a = slot[r], b = slot[r + 1];
-                    slot[r] = a < b ? a : b;
-                    slot[r + 1] = a < b ? b : a;
-                }
-            } else {
-#pragma unroll
-                for (int r = 0; r < R; ++r) {
-                    const unsigned long long p = __shfl_xor_sync(0xFFFFFFFFu, slot[r], stride);
-                    const bool lower = (lane & stride) == 0;
-                    const bool p_less = p < slot[r];
-                    slot[r] = (lower == p_less) ? p : slot[r];
-                }
-            }
-        }
+    __device__ __forceinline__ unsigned long long worst() const {
+        return __shfl_sync(0xFFFFFFFFu, slot[RS - 1], 3, 4);
     }
 };
+
 
 template <int MODE, int KP, int CH>
 struct Tc5Shape {
@@ -453,8 +400,9 @@ __global__ void __launch_bounds__(kT5Threads, 1) k_tc5_select(const Tc5Args a) {
     __shared__ uint32_t tmem_base_sh;
     __shared__ int abort_sh;
     constexpr int C = 2 * CH;                 // over-fetch per row and slice
-    constexpr int R = C <= 32 ? 1 : C / 32;   // list registers per lane
+    constexpr int RS = C / 4;                 // list keys per lane (4 lanes per row)
     constexpr int ROWS_PER_WARP = kT5Rows / kT5EpiWarps;
+    static_assert(ROWS_PER_WARP * 4 == 32, "one row per group of 4 lanes");
     constexpr int NEPI = 32 * kT5EpiWarps;
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -576,20 +524,18 @@ __global__ void __launch_bounds__(kT5Threads, 1) k_tc5_select(const Tc5Args a) {
         // key of its over-fetch list, possibly stale but never too small);
         // the rare hits are appended to the row's buffer in shared memory.
         // After a tile, warp w merges the buffers of rows 8w .. 8w+7 into
-        // their lists (kept in its registers) and publishes the new
-        // thresholds.  A row can take at most kT5Buf hits per tile on this
+        // their lists (kept in its registers, one row per group of 4 lanes)
+        // and publishes the new thresholds.  A row can take at most kT5Buf hits per tile on this
         // path; a tile that overflows a buffer (the first tiles of a slice,
         // while the lists fill) is done again from tensor memory in four
         // phases of 64 columns, merging after each, which cannot overflow.
         const int quarter = warp & 3, cgroup = warp >> 2;
         const int myrow = 32 * quarter + lane;
-        RowList<R> lists[ROWS_PER_WARP];
-        unsigned long long worst[ROWS_PER_WARP];
-#pragma unroll
-        for (int i = 0; i < ROWS_PER_WARP; ++i) {
-            lists[i].init(C, lane);
-            worst[i] = kScoreSentinel;
-        }
+        const int grow = warp * ROWS_PER_WARP + (lane >> 2);  // the row this lane's group keeps
+        const int gl = lane & 3;
+        GroupList<RS> glist;
+        glist.init();
+        unsigned long long gworst = kScoreSentinel;
         const uint32_t trow = tmem + (uint32_t(32 * quarter) << 16);
         constexpr int NPHASE = kT5Cols / kT5Chunk;
         if (tid < kT5Rows) {
@@ -611,46 +557,24 @@ __global__ void __launch_bounds__(kT5Threads, 1) k_tc5_select(const Tc5Args a) {
                 }
             }
         };
-        // merge the buffered hits of this warp's rows into their lists
+        // merge the buffered hits of this warp's rows into their lists: the 8
+        // rows side by side, one hit of each row per step (a row out of hits
+        // offers the sentinel); a step no row can use is skipped
         auto merge = [&]() {
-#pragma unroll
-            for (int i = 0; i < ROWS_PER_WARP; ++i) {
-                const int row = warp * ROWS_PER_WARP + i;
-                const int n = min(sCnt[row], kT5Buf);
-                if (n == 0) continue;  // uniform: every lane read the same count
-                const unsigned long long* B = sBuf + row * kT5BufStride;
-                if (n >= kT5BatchMin) {
-                    // many hits (while the list fills): one sorted merge per 32 R of them
-                    for (int b0 = 0; b0 < n; b0 += 32 * R) {
-                        unsigned long long x[R];
-#pragma unroll
-                        for (int r = 0; r < R; ++r) {
-                            const int e = b0 + r * 32 + lane;
-                            x[r] = e < n ? B[e] : kScoreSentinel;
-                        }
-                        lists[i].merge_batch(x, lane);
-                    }
-                    worst[i] = lists[i].worst();
-                } else {
-                    for (int b0 = 0; b0 < n; b0 += 32) {
-                        const unsigned long long key = b0 + lane < n ? B[b0 + lane] : kScoreSentinel;
-                        unsigned m = __ballot_sync(0xFFFFFFFFu, key < worst[i]);
-                        while (m) {
-                            const int src = __ffs(m) - 1;
-                            m &= m - 1;
-                            const unsigned long long c = __shfl_sync(0xFFFFFFFFu, key, src);
-                            if (c < worst[i]) {
-                                lists[i].insert(c, lane);
-                                worst[i] = lists[i].worst();
-                            }
-                        }
-                    }
+            const int n = min(sCnt[grow], kT5Buf);  // the same on the 4 lanes of a group
+            const unsigned long long* B = sBuf + grow * kT5BufStride;
+            const int nmax = __reduce_max_sync(0xFFFFFFFFu, n);
+            for (int h = 0; h < nmax; ++h) {
+                const unsigned long long c = h < n ? B[h] : kScoreSentinel;
+                if (__any_sync(0xFFFFFFFFu, c < gworst)) {
+                    glist.insert(c, gl);
+                    gworst = glist.worst();
                 }
-                __syncwarp();
-                if (lane == 0) {
-                    sCnt[row] = 0;
-                    sThr[row] = key_score(worst[i]);
-                }
+            }
+            __syncwarp();
+            if (gl == 0 && n > 0) {
+                sCnt[grow] = 0;
+                sThr[grow] = key_score(gworst);
             }
         };
         for (int t = 0; t < ntiles; ++t) {
@@ -711,24 +635,18 @@ __global__ void __launch_bounds__(kT5Threads, 1) k_tc5_select(const Tc5Args a) {
             }
         }
         // write the lists: C candidates per row and the row threshold
-#pragma unroll
-        for (int i = 0; i < ROWS_PER_WARP; ++i) {
-            const int row = warp * ROWS_PER_WARP + i;
-            const int q = blockIdx.x * kT5Rows + row;
+        {
+            const int q = blockIdx.x * kT5Rows + grow;
             if (q < a.nq) {
-                const long long base = ((long long)q * a.nsplit + blockIdx.y) * C;
+                const long long base = ((long long)q * a.nsplit + blockIdx.y) * C + RS * gl;
 #pragma unroll
-                for (int r = 0; r < R; ++r) {
-                    const int sidx = r * 32 + lane;
-                    const int o = sidx - (32 * R - C);
-                    if (o >= 0) {
-                        const unsigned long long key = lists[i].slot[r];
-                        const bool real = key != kScoreSentinel;
-                        a.cand_s[base + o] = key_score(key);
-                        a.cand_i[base + o] = real ? int32_t(uint32_t(key)) : -1;
-                    }
+                for (int i = 0; i < RS; ++i) {
+                    const unsigned long long key = glist.slot[i];
+                    const bool real = key != kScoreSentinel;
+                    a.cand_s[base + i] = key_score(key);
+                    a.cand_i[base + i] = real ? int32_t(uint32_t(key)) : -1;
                 }
-                if (lane == 0) a.tau[(long long)q * a.nsplit + blockIdx.y] = key_score(worst[i]);
+                if (gl == 0) a.tau[(long long)q * a.nsplit + blockIdx.y] = key_score(gworst);
             }
         }
     }
