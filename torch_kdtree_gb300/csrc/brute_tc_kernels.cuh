@@ -547,10 +547,11 @@ __global__ void __launch_bounds__(kT5Threads, 1) k_tc5_select(const Tc5Args a) {
         bar_epi();
         unsigned long long* myBuf = sBuf + myrow * kT5BufStride;
         // compare 16 scores of columns col0 .. col0+15 with thr, append the hits
-        auto append16 = [&](const float (&v)[16], int col0, float thr, int* ovf) {
+        // (`edge`: the columns may run past the slice's end, in its last tile)
+        auto append16 = [&](const float (&v)[16], int col0, float thr, int* ovf, bool edge) {
 #pragma unroll
             for (int i = 0; i < 16; ++i) {
-                if (v[i] <= thr && col0 + i < r1) {
+                if (v[i] <= thr && (!edge || col0 + i < r1)) {
                     const int pos = atomicAdd(&sCnt[myrow], 1);
                     if (pos < kT5Buf) myBuf[pos] = score_key(v[i], uint32_t(col0 + i));
                     else *ovf = 1;
@@ -592,11 +593,14 @@ __global__ void __launch_bounds__(kT5Threads, 1) k_tc5_select(const Tc5Args a) {
             if (w_ok) {
                 sm100::tc_fence_after();
                 const float thr = sThr[myrow];
+                const bool edge = base + kT5Cols > r1;
 #pragma unroll
-                for (int j = 0; j < NPHASE; ++j) {
-                    float v[16];
-                    sm100::tmem_ld16(tcol + uint32_t(j * kT5Chunk + cgroup * 16), v);
-                    append16(v, base + j * kT5Chunk + cgroup * 16, thr, &sFlag[par]);
+                for (int j = 0; j < NPHASE; j += 2) {
+                    float v0[16], v1[16];
+                    sm100::tmem_ld16x2(tcol + uint32_t(j * kT5Chunk + cgroup * 16),
+                                       tcol + uint32_t((j + 1) * kT5Chunk + cgroup * 16), v0, v1);
+                    append16(v0, base + j * kT5Chunk + cgroup * 16, thr, &sFlag[par], edge);
+                    append16(v1, base + (j + 1) * kT5Chunk + cgroup * 16, thr, &sFlag[par], edge);
                 }
             } else if (lane == 0) {
                 sFlag[2 + par] = 1;
@@ -617,7 +621,7 @@ __global__ void __launch_bounds__(kT5Threads, 1) k_tc5_select(const Tc5Args a) {
                         float v[16];
                         sm100::tmem_ld16(tcol + uint32_t(j * kT5Chunk + cgroup * 16), v);
                         int dummy = 0;
-                        append16(v, base + j * kT5Chunk + cgroup * 16, thr, &dummy);  // <= 64 hits per row
+                        append16(v, base + j * kT5Chunk + cgroup * 16, thr, &dummy, true);  // <= 64 hits per row
                         bar_epi();
                         merge();
                         bar_epi();
