@@ -210,8 +210,8 @@ int tk_tree_query_noalloc(const tk_tree* tree, const void* q, int64_t nq, int k,
 typedef struct tk_batch tk_batch;
 
 /* Plan a batched query over n_trees clouds, each with its own tree (same
- * dtype, dims and device; dims 1..3 -- wider trees are queried one by one)
- * and its own k (ks[c], 1..min(n_c, 128)); query
+ * dtype, dims and device; dims 1..8) and its own k (ks[c], 1..min(n_c,
+ * 128)); query
  * counts per cloud are fixed by q_counts.  The trees must outlive the batch.
  * Queries are passed concatenated cloud after cloud ([sum q_counts, dims]);
  * results come back concatenated the same way, cloud c occupying a
@@ -226,8 +226,10 @@ int64_t tk_batch_output_size(const tk_batch* batch);
 /* All clouds in one persistent launch fed by a global work counter (plus
  * the binning kernels).  Device work only, no host synchronisation and no
  * allocation: it can be captured in a CUDA graph.  threads_per_query: 0 =
- * auto, 1 (max k <= 16) or 8.  prune_boxes: ignored (kept for binary
- * compatibility): the batched search always prunes with node bounding boxes. */
+ * auto, 1 (max k <= 16), or 8 / 32 (any k): trees of 1-3 dims run groups
+ * of 8 lanes, trees of 4-8 dims groups of 32 (their kernels' shapes).
+ * prune_boxes: trees of 1-3 dims always prune with node bounding boxes
+ * (the argument is kept for binary compatibility); trees of 4-8 dims too. */
 int tk_batch_query(const tk_batch* batch, const void* q, void* dists, int32_t* idx, int threads_per_query,
                    int prune_boxes, void* workspace, size_t workspace_bytes, void* stream);
 

@@ -25,15 +25,17 @@ def torch_indexed_grads(q, ref, inds, w):
 
 
 @pytest.mark.parametrize("dtype,tol", [(torch.float32, 1e-5), (torch.float64, 1e-12)])
-@pytest.mark.parametrize("d", [1, 2, 3, 5, 8])
+@pytest.mark.parametrize("d", [1, 2, 3, 5, 8, 12, 40])
 def test_matches_torch_indexed_gradient(dtype, tol, d):
     g = torch.Generator(device="cpu").manual_seed(7)
     ref = torch.randn(20000, d, generator=g, dtype=dtype).to(cuda).requires_grad_(True)
     q = torch.randn(30000, d, generator=g, dtype=dtype).to(cuda).requires_grad_(True)
     k = 8
     w = torch.rand(30000, k, generator=g, dtype=dtype).to(cuda)
-    tree = tk().build_kd_tree(ref)
-    dists, inds = tree.query(q, nr_nns_searches=k)
+    if d <= 8:
+        dists, inds = tk().build_kd_tree(ref).query(q, nr_nns_searches=k)
+    else:  # KD trees stop at 8 dims; the exhaustive search has the same backward
+        dists, inds = tk().nn_distance(ref, q, k)
     (0.5 * (dists * w).sum()).backward()
     gq_t, gr_t = torch_indexed_grads(q, ref, inds, w)
     scale_q = gq_t.abs().max().item()
@@ -102,17 +104,19 @@ def test_finite_differences_fp64():
             assert abs(an - fd) <= 1e-3 * max(abs(fd), 1e-3), (m, c, an, fd)
 
 
+@pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
 @pytest.mark.parametrize("d", [3, 6, 16])
-def test_hub_segments_are_deterministic_and_accurate(d):
+def test_hub_segments_are_deterministic_and_accurate(d, dtype):
     """Every query shares the same few neighbours (segments of 100,000+ pairs):
-    the order-independent fixed-point sums (d <= 8) and the sorted segments
-    (d = 16) give the same bits on every run and match an FP64 sum."""
+    the order-independent fixed-point sums (64-bit integers for float32
+    terms, 128-bit for float64; 8 coordinates per pass) give the same bits on
+    every run and match a sum in higher precision."""
     g = torch.Generator(device="cpu").manual_seed(9)
-    ref = torch.randn(5000, d, generator=g)
-    ref[:8] = 40.0 + torch.randn(8, d, generator=g) * 1e-3  # a far-away cluster of 8 points
-    q = 40.0 + torch.randn(120000, d, generator=g) * 1e-2    # all queries next to it
+    ref = torch.randn(5000, d, generator=g, dtype=dtype)
+    ref[:8] = 40.0 + torch.randn(8, d, generator=g, dtype=dtype) * 1e-3  # a far-away cluster of 8 points
+    q = 40.0 + torch.randn(120000, d, generator=g, dtype=dtype) * 1e-2    # all queries next to it
     ref, q = ref.to(cuda), q.to(cuda)
-    w = torch.rand(120000, 8, generator=g).to(cuda)
+    w = torch.rand(120000, 8, generator=g, dtype=dtype).to(cuda)
     outs = []
     for _ in range(3):
         r = ref.clone().requires_grad_(True)
@@ -123,13 +127,14 @@ def test_hub_segments_are_deterministic_and_accurate(d):
     assert (inds.long() < 8).all()
     for gr in outs[1:]:
         assert torch.equal(gr, outs[0])
-    # FP64 sum of the same terms
-    r64, q64, w64 = ref.double(), q.double(), w.double()
-    terms = (w64[..., None] * (r64[inds.long()] - q64[:, None]))  # 2 * 0.5 * w * (r - q)
-    exact = torch.zeros_like(r64).index_add_(0, inds.long().reshape(-1), terms.reshape(-1, d))
-    err = (outs[0].double() - exact).abs().max().item()
-    # fixed-point sums: one rounding; sorted segments (d = 16): a sequential FP32 sum of ~120,000 terms
-    assert err <= (1e-5 if d <= 8 else 1e-3) * exact.abs().max().item()
+    # the same terms summed in higher precision (FP64 for float32 terms; for
+    # float64 terms, FP64 of the rounded terms on the CPU in a fixed order)
+    il = inds.long().cpu()
+    terms = (w.double().cpu()[..., None] * (ref.double().cpu()[il] - q.double().cpu()[:, None]))
+    exact = torch.zeros(ref.shape, dtype=torch.float64).index_add_(0, il.reshape(-1), terms.reshape(-1, d))
+    err = (outs[0].double().cpu() - exact).abs().max().item()
+    # fixed-point sums: one rounding of a sum far more precise than the terms
+    assert err <= (1e-5 if dtype == torch.float32 else 1e-12) * exact.abs().max().item()
 
 
 def test_no_queries_gives_zero_reference_gradient():

@@ -64,3 +64,32 @@ def test_batch_errors():
     b = BatchedKDTrees([r], [2], [4])
     with pytest.raises(Exception):
         b.query_flat(torch.randn(5, 3, device=cuda))  # wrong query count
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+@pytest.mark.parametrize("dims", [4, 5, 6, 7, 8])
+@pytest.mark.parametrize("tpq", [0, 1, 32])
+def test_batch_of_wide_trees(dtype, dims, tpq, oracle):
+    """Trees of 4-8 dimensions batched in one launch: the same bits as one
+    query per cloud and as the oracle's exhaustive search, ties included."""
+    from torch_kdtree_gb300.batched import BatchedKDTrees
+    rng = np.random.default_rng(100 + dims)
+    sizes = (40, 3000, 20000, 700, 9)
+    refs_np = [rng.standard_normal((n, dims)).astype(dtype) for n in sizes]
+    refs_np[1][:200] = refs_np[1][200:400]  # exact duplicates: ties
+    qs_np = [rng.standard_normal((n, dims)).astype(dtype) for n in (30, 1200, 0, 500, 9)]
+    ks = [5, 16, 1, 3, 9] if tpq == 1 else [5, 40, 1, 128, 9]
+    levels = [None, 9, 11, None, 1]
+    b = BatchedKDTrees([torch.from_numpy(r).to(cuda) for r in refs_np], ks, [len(q) for q in qs_np],
+                       levels=levels, threads_per_query=tpq)
+    qs = [torch.from_numpy(q).to(cuda) for q in qs_np]
+    d_b, i_b = b.query(qs)
+    b.query_each(qs)
+    for c, (r, q, k, db, ib, de, ie) in enumerate(zip(refs_np, qs_np, ks, d_b, i_b, b.split(b.out_dists),
+                                                      b.split(b.out_idx))):
+        if len(q) == 0:
+            continue
+        assert torch.equal(db, de) and torch.equal(ib, ie), c
+        bd, bi = oracle.brute(r, q, k)
+        np.testing.assert_array_equal(db.cpu().numpy(), bd)
+        np.testing.assert_array_equal(ib.cpu().numpy(), bi)

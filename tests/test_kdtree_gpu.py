@@ -253,7 +253,8 @@ def test_wide_trees_every_shape(dims, dtype, oracle):
 
 def test_wide_tree_build_save_load_and_grad(tmp_path, oracle):
     """GPU build, host build and a saved / re-loaded tree agree for a wide
-    cloud; gradients flow as for 3-D trees; batches refuse wide trees."""
+    cloud; gradients flow as for 3-D trees; a batch of the wide tree answers
+    like the tree itself."""
     rng = np.random.default_rng(66)
     ref = rng.standard_normal((20000, 6)).astype(np.float32)
     q = rng.standard_normal((3000, 6)).astype(np.float32)
@@ -274,8 +275,10 @@ def test_wide_tree_build_save_load_and_grad(tmp_path, oracle):
     d.sum().backward()
     assert torch.allclose(qg.grad, 2 * (qg[:, None] - rt[i.long()]).sum(1))
     from torch_kdtree_gb300.batched import BatchedKDTrees
-    with pytest.raises(Exception):
-        BatchedKDTrees([rt], [4], [10])
+    b = BatchedKDTrees([rt], [4], [10])
+    (db,), (ib,) = b.query([qt[:10]])
+    d4, i4 = td.query(qt[:10], nr_nns_searches=4)
+    assert torch.equal(db, d4) and torch.equal(ib, i4)
 
 
 def _non_finite_rows(q):

@@ -7,7 +7,8 @@ persistent launch (tk_batch_* in include/tk_knn.h).
     replay()                                         # -> trees.out_dists / trees.out_idx (flat)
 
 The reference queried one cloud per call; this is the batched pattern of the
-engine, equivalent bit for bit to querying every tree on its own.
+engine, equivalent bit for bit to querying every tree on its own.  Trees of
+1-8 dimensions (one dims per batch).
 """
 from __future__ import annotations
 

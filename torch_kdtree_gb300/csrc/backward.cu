@@ -8,18 +8,14 @@
 //   grad_q[i]   = sum_j 2 g[i, j] (q[i] - ref[idx[i, j]])       (a gather, j ascending)
 //   grad_ref[m] = sum_{(i,j): idx[i,j] = m} 2 g[i, j] (ref[m] - q[i])
 // grad_ref is a segmented reduction over the indices, bitwise reproducible and
-// without float atomics, in one of two forms:
-//  * float32, d <= 8: segments are built by counting (integer atomics, whose
-//    returned ranks then place each pair), so the order inside a segment is
-//    arbitrary; the segment's sum is made order-independent instead.  One
-//    pass finds the
-//    largest exponent of its terms per coordinate, a second adds every FP32
-//    term exactly as a 64-bit fixed-point integer scaled to that exponent,
-//    and the total is rounded once -- the same bits whatever the order, and
-//    closer to the exact sum than a sequential FP32 sum;
-//  * otherwise: the (idx, pair) list is sorted by a stable radix sort, so
-//    each reference point sees its pairs in ascending pair order and one
-//    thread sums them in that fixed order.
+// without float atomics: segments are built by counting (integer atomics,
+// whose returned ranks then place each pair), so the order inside a segment
+// is arbitrary, and the segment's sum is made order-independent instead.  One
+// pass finds the largest exponent of its terms per coordinate, a second adds
+// every term as a fixed-point integer scaled to that exponent (64-bit for
+// float32 terms, 128-bit for float64), and the total is rounded once -- the
+// same bits whatever the order, and closer to the exact sum than a sequential
+// sum in the terms' own precision.  Coordinates go 8 per pass (registers).
 // Differences are recomputed from the saved indices; nothing of size
 // [Q, k, d] is stored.
 #include <algorithm>
@@ -58,57 +54,7 @@ __global__ void k_grad_q(const T* __restrict__ q, const T* __restrict__ ref, con
         if (c < d) grad_q[(long long)i * d + c] = acc[c];
 }
 
-// keys: neighbour index (n for invalid entries, which sort last).
-__global__ void k_make_keys(const int32_t* __restrict__ idx, long long npairs, int n, uint32_t* __restrict__ keys) {
-    const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= npairs) return;
-    const int m = idx[p];
-    keys[p] = (m < 0 || m >= n) ? uint32_t(n) : uint32_t(m);
-}
-
-// Segment bounds of every key present in the sorted list: seg_start[m] and
-// seg_end[m] (one past the last position).  Keys absent from the list keep
-// seg_end[m] = 0 (zeroed beforehand) and are skipped.
-__global__ void k_segment_bounds(const uint32_t* __restrict__ keys, long long npairs, int n,
-                                 int* __restrict__ seg_start, int* __restrict__ seg_end) {
-    const long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= npairs) return;
-    const uint32_t key = keys[s];
-    if (key >= uint32_t(n)) return;
-    if (s == 0 || keys[s - 1] != key) seg_start[key] = int(s);
-    if (s == npairs - 1 || keys[s + 1] != key) seg_end[key] = int(s + 1);
-}
-
-// One thread per reference point walks its segment in sorted (ascending
-// pair) order.
-template <typename T, int D>
-__global__ void k_grad_ref(const T* __restrict__ q, const T* __restrict__ ref, const T* __restrict__ g,
-                           const uint32_t* __restrict__ pairs, const int* __restrict__ seg_start,
-                           const int* __restrict__ seg_end, int n, int k, int d, T* __restrict__ grad_ref) {
-    const int m = blockIdx.x * blockDim.x + threadIdx.x;
-    if (m >= n) return;
-    T rm[D], acc[D];
-#pragma unroll
-    for (int c = 0; c < D; ++c) {
-        rm[c] = c < d ? ref[(long long)m * d + c] : T(0);
-        acc[c] = T(0);
-    }
-    const int end = seg_end[m];
-    const int beg = end > 0 ? seg_start[m] : 0;  // seg_start is only written for keys present
-    for (int s = beg; s < end; ++s) {
-        const uint32_t p = pairs[s];
-        const long long i = (long long)(p / uint32_t(k));
-        const T w = T(2) * g[p];
-#pragma unroll
-        for (int c = 0; c < D; ++c)
-            if (c < d) acc[c] += w * (rm[c] - q[i * d + c]);
-    }
-#pragma unroll
-    for (int c = 0; c < D; ++c)
-        if (c < d) grad_ref[(long long)m * d + c] = acc[c];
-}
-
-// Segments by counting (float32, d <= 8): counts of every key (then their
+// Segments by counting: counts of every key (then their
 // exclusive scan, n + 1 entries: starts, and the total at n), and each pair's
 // arrival rank within its key, which places it in the segment without a
 // second round of atomics.
@@ -162,16 +108,18 @@ __device__ __forceinline__ long long to_fixed(float t, int sh) {
 // below 2^61, so the int64 accumulator cannot overflow.  Each scaled term is
 // rounded to an integer once (to_fixed), by a rule that does not depend on
 // the order.
-// D: compile-time bound of the runtime dimension d (d <= D <= 8).
+// This pass: coordinates c0 .. c0 + dc - 1, dc = min(D, d - c0) <= 8.
 template <int D>
 __global__ void k_grad_ref_fixed(const float* __restrict__ q, const float* __restrict__ ref, const float* __restrict__ g,
                                  const uint32_t* __restrict__ list, const int* __restrict__ starts, int n, int k, int d,
-                                 float* __restrict__ grad_ref) {
+                                 int c0, float* __restrict__ grad_ref) {
     const int m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= n) return;
+    const int dc = min(D, d - c0);
+    q += c0;
     float rm[D];
 #pragma unroll
-    for (int c = 0; c < D; ++c) rm[c] = c < d ? ref[(long long)m * d + c] : 0.f;
+    for (int c = 0; c < D; ++c) rm[c] = c < dc ? ref[(long long)m * d + c0 + c] : 0.f;
     const int s0 = starts[m], s1 = starts[m + 1];
     int emax[D];
 #pragma unroll
@@ -188,7 +136,7 @@ __global__ void k_grad_ref_fixed(const float* __restrict__ q, const float* __res
             const float w = 2.f * g[p];
 #pragma unroll
             for (int c = 0; c < D; ++c) {
-                keep[u][c] = __fmul_rn(w, __fsub_rn(rm[c], (c < d ? q[i * d + c] : rm[c])));
+                keep[u][c] = __fmul_rn(w, __fsub_rn(rm[c], (c < dc ? q[i * d + c] : rm[c])));
                 const int e = exp_field(keep[u][c]);
                 finite = finite && e != 255;
                 emax[c] = max(emax[c], e);
@@ -201,7 +149,7 @@ __global__ void k_grad_ref_fixed(const float* __restrict__ q, const float* __res
         const float w = 2.f * g[p];
 #pragma unroll
         for (int c = 0; c < D; ++c) {
-            const int e = exp_field(__fmul_rn(w, __fsub_rn(rm[c], (c < d ? q[i * d + c] : rm[c]))));
+            const int e = exp_field(__fmul_rn(w, __fsub_rn(rm[c], (c < dc ? q[i * d + c] : rm[c]))));
             finite = finite && e != 255;
             emax[c] = max(emax[c], e);
         }
@@ -216,7 +164,7 @@ __global__ void k_grad_ref_fixed(const float* __restrict__ q, const float* __res
             const long long i = (long long)(p / uint32_t(k));
             const float w = 2.f * g[p];
 #pragma unroll
-            for (int c = 0; c < D; ++c) out[c] += __fmul_rn(w, __fsub_rn(rm[c], (c < d ? q[i * d + c] : rm[c])));
+            for (int c = 0; c < D; ++c) out[c] += __fmul_rn(w, __fsub_rn(rm[c], (c < dc ? q[i * d + c] : rm[c])));
         }
     } else {
         const int L = 32 - __clz(s1 - s0);  // s1 - s0 < 2^L
@@ -234,47 +182,130 @@ __global__ void k_grad_ref_fixed(const float* __restrict__ q, const float* __res
             const float w = 2.f * g[p];
 #pragma unroll
             for (int c = 0; c < D; ++c)
-                acc[c] += to_fixed(__fmul_rn(w, __fsub_rn(rm[c], (c < d ? q[i * d + c] : rm[c]))), 187 - L - emax[c]);
+                acc[c] += to_fixed(__fmul_rn(w, __fsub_rn(rm[c], (c < dc ? q[i * d + c] : rm[c]))), 187 - L - emax[c]);
         }
 #pragma unroll
         for (int c = 0; c < D; ++c) out[c] = float(double(acc[c]) * pow2(emax[c] + L - 187));
     }
 #pragma unroll
     for (int c = 0; c < D; ++c)
-        if (c < d) grad_ref[(long long)m * d + c] = out[c];
+        if (c < dc) grad_ref[(long long)m * d + c0 + c] = out[c];
 }
 
+
+// Exponent field of a double (0 for zeros and subnormals, 2047 for inf / NaN).
+__device__ __forceinline__ int exp_field64(double t) { return int((__double_as_longlong(t) >> 52) & 0x7FF); }
+
+// t * 2^sh rounded to the nearest integer (halves away from zero), in integer
+// arithmetic: a finite double is mant * 2^(max(e, 1) - 1075) with its 53-bit
+// significand mant.  The caller guarantees |t * 2^sh| < 2^124.
+__device__ __forceinline__ __int128 to_fixed64(double t, int sh) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(t);
+    const int e = int((b >> 52) & 0x7FFu);
+    const long long mant = (long long)((b & 0xFFFFFFFFFFFFFull) | (e ? (1ull << 52) : 0ull));
+    const int amt = (e ? e : 1) - 1075 + sh;
+    __int128 v;
+    if (amt >= 0)
+        v = (__int128)mant << amt;
+    else if (amt > -54)
+        v = (__int128)((mant + (1ll << (-amt - 1))) >> (-amt));
+    else
+        v = 0;  // below half a unit
+    return (b >> 63) ? -v : v;
+}
+
+// The float64 form of k_grad_ref_fixed: a term t has |t| < 2^(E - 1022) for
+// the largest exponent field E of its coordinate (E >= 1); scaled by
+// 2^(1146 - L - E), with s < 2^L terms, each scaled term is below 2^(124 - L)
+// and the sum below 2^124: a 128-bit accumulator cannot overflow, and every
+// term keeps 71 - L bits below the largest term's leading bit.
+template <int D>
+__global__ void k_grad_ref_fixed64(const double* __restrict__ q, const double* __restrict__ ref,
+                                   const double* __restrict__ g, const uint32_t* __restrict__ list,
+                                   const int* __restrict__ starts, int n, int k, int d, int c0,
+                                   double* __restrict__ grad_ref) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= n) return;
+    const int dc = min(D, d - c0);
+    q += c0;
+    double rm[D];
+#pragma unroll
+    for (int c = 0; c < D; ++c) rm[c] = c < dc ? ref[(long long)m * d + c0 + c] : 0.0;
+    const int s0 = starts[m], s1 = starts[m + 1];
+    int emax[D];
+#pragma unroll
+    for (int c = 0; c < D; ++c) emax[c] = 1;
+    bool finite = true;
+    for (int j = s0; j < s1; ++j) {
+        const uint32_t p = list[j];
+        const long long i = (long long)(p / uint32_t(k));
+        const double w = 2.0 * g[p];
+#pragma unroll
+        for (int c = 0; c < D; ++c) {
+            const int e = exp_field64(__dmul_rn(w, __dsub_rn(rm[c], (c < dc ? q[i * d + c] : rm[c]))));
+            finite = finite && e != 2047;
+            emax[c] = max(emax[c], e);
+        }
+    }
+    double out[D];
+    if (!finite) {
+        // an infinite or NaN term: the sum is +-inf or NaN in any order
+#pragma unroll
+        for (int c = 0; c < D; ++c) out[c] = 0.0;
+        for (int j = s0; j < s1; ++j) {
+            const uint32_t p = list[j];
+            const long long i = (long long)(p / uint32_t(k));
+            const double w = 2.0 * g[p];
+#pragma unroll
+            for (int c = 0; c < D; ++c) out[c] += __dmul_rn(w, __dsub_rn(rm[c], (c < dc ? q[i * d + c] : rm[c])));
+        }
+    } else {
+        const int L = 32 - __clz(s1 - s0);  // s1 - s0 < 2^L
+        __int128 acc[D];
+#pragma unroll
+        for (int c = 0; c < D; ++c) acc[c] = 0;
+        for (int j = s0; j < s1; ++j) {
+            const uint32_t p = list[j];
+            const long long i = (long long)(p / uint32_t(k));
+            const double w = 2.0 * g[p];
+#pragma unroll
+            for (int c = 0; c < D; ++c)
+                acc[c] += to_fixed64(__dmul_rn(w, __dsub_rn(rm[c], (c < dc ? q[i * d + c] : rm[c]))),
+                                     1146 - L - emax[c]);
+        }
+#pragma unroll
+        for (int c = 0; c < D; ++c) {
+            const bool neg = acc[c] < 0;
+            const unsigned __int128 mag = neg ? (unsigned __int128)(-acc[c]) : (unsigned __int128)acc[c];
+            const double v = ldexp(double((unsigned long long)(mag >> 64)), 64) + double((unsigned long long)mag);
+            out[c] = ldexp(neg ? -v : v, emax[c] + L - 1146);
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < D; ++c)
+        if (c < dc) grad_ref[(long long)m * d + c0 + c] = out[c];
+}
+
+// Workspace: each pair's rank within its key, the segment list, the n + 1
+// counts / segment starts and the scan's scratch.
 struct BwLayout {
-    size_t keys = 0, sorted_keys = 0, sorted_vals = 0, seg_end = 0, seg_start = 0, sort_ws = 0, scan_ws = 0,
-           total = 0;
+    size_t rank = 0, list = 0, starts = 0, scan_ws = 0, total = 0;
 };
 
 BwLayout bw_layout(int64_t nq, int k, int64_t n) {
     BwLayout w;
     const int64_t np = std::max<int64_t>(1, nq * k);
     size_t o = 0;
-    w.keys = o;
+    w.rank = o;
     o += align256(4 * size_t(np));
-    w.sorted_keys = o;
+    w.list = o;
     o += align256(4 * size_t(np));
-    w.sorted_vals = o;
-    o += align256(4 * size_t(np));
-    w.seg_end = o;  // also the n + 1 counts / starts of the counting path
+    w.starts = o;
     o += align256(4 * size_t(std::max<int64_t>(n, 1) + 1));
-    w.seg_start = o;
-    o += align256(4 * size_t(std::max<int64_t>(n, 1)));
-    w.sort_ws = o;
-    o += sort_workspace_bytes(np);
     w.scan_ws = o;
     o += scan_workspace_bytes(std::max<int64_t>(n, 1) + 1);
     w.total = o;
     return w;
-}
-
-int key_bits_for(int64_t n) {
-    int b = 1;
-    while ((int64_t(1) << b) <= n) ++b;  // keys 0..n inclusive (n marks invalid)
-    return b;
 }
 
 template <typename T, int D>
@@ -282,41 +313,31 @@ int run_backward(const T* q, const T* ref, const int32_t* idx, const T* g, int n
                  T* grad_ref, char* ws, cudaStream_t s) {
     const int bs = D > 32 ? 64 : 256;
     if (grad_q && nq > 0) k_grad_q<T, D><<<(nq + bs - 1) / bs, bs, 0, s>>>(q, ref, idx, g, nq, n, k, d, grad_q);
-    if (grad_ref && sizeof(T) == 4 && D <= 8) {
+    if (grad_ref) {
         const BwLayout w = bw_layout(nq, k, n);
         const long long np = (long long)nq * k;
-        int* starts = reinterpret_cast<int*>(ws + w.seg_end);  // n + 1
-        int* rank = reinterpret_cast<int*>(ws + w.keys);        // np
-        uint32_t* list = reinterpret_cast<uint32_t*>(ws + w.sorted_vals);
+        int* starts = reinterpret_cast<int*>(ws + w.starts);  // n + 1
+        int* rank = reinterpret_cast<int*>(ws + w.rank);      // np
+        uint32_t* list = reinterpret_cast<uint32_t*>(ws + w.list);
         cudaError_t e = cudaMemsetAsync(starts, 0, sizeof(int) * (size_t(n) + 1), s);
         if (e != cudaSuccess) return fail(TK_ECUDA, std::string("memset: ") + cudaGetErrorString(e));
         if (np > 0) k_count_keys<<<unsigned((np + 255) / 256), 256, 0, s>>>(idx, np, n, starts, rank);
         e = exclusive_scan(starts, int64_t(n) + 1, ws + w.scan_ws, s);
         if (e != cudaSuccess) return fail(TK_ECUDA, std::string("backward scan: ") + cudaGetErrorString(e));
         if (np > 0) k_fill_segments<<<unsigned((np + 255) / 256), 256, 0, s>>>(idx, np, n, starts, rank, list);
-        if constexpr (sizeof(T) == 4 && D <= 8)
-            k_grad_ref_fixed<D><<<(n + 255) / 256, 256, 0, s>>>(reinterpret_cast<const float*>(q),
-                                                                 reinterpret_cast<const float*>(ref),
-                                                                 reinterpret_cast<const float*>(g), list, starts, n, k,
-                                                                 d, reinterpret_cast<float*>(grad_ref));
-    } else if (grad_ref) {
-        const BwLayout w = bw_layout(nq, k, n);
-        const long long np = (long long)nq * k;
-        uint32_t* keys = reinterpret_cast<uint32_t*>(ws + w.keys);
-        uint32_t* sk = reinterpret_cast<uint32_t*>(ws + w.sorted_keys);
-        uint32_t* sv = reinterpret_cast<uint32_t*>(ws + w.sorted_vals);
-        int* seg_end = reinterpret_cast<int*>(ws + w.seg_end);
-        int* seg_start = reinterpret_cast<int*>(ws + w.seg_start);
-        if (np > 0) {
-            k_make_keys<<<unsigned((np + 255) / 256), 256, 0, s>>>(idx, np, n, keys);
-            cudaError_t e = sort_pairs(keys, nullptr, sk, sv, np, key_bits_for(n), ws + w.sort_ws,
-                                       sort_workspace_bytes(np), s);
-            if (e != cudaSuccess) return fail(TK_ECUDA, std::string("backward sort: ") + cudaGetErrorString(e));
+        // coordinates 8 per pass (one pass up to 8 dims; D = 1..3 keep their exact width)
+        constexpr int DC = D <= 3 ? D : 8;
+        for (int c0 = 0; c0 < d; c0 += DC) {
+            if constexpr (sizeof(T) == 4)
+                k_grad_ref_fixed<DC><<<(n + 255) / 256, 256, 0, s>>>(
+                    reinterpret_cast<const float*>(q), reinterpret_cast<const float*>(ref),
+                    reinterpret_cast<const float*>(g), list, starts, n, k, d, c0, reinterpret_cast<float*>(grad_ref));
+            else
+                k_grad_ref_fixed64<DC><<<(n + 255) / 256, 256, 0, s>>>(
+                    reinterpret_cast<const double*>(q), reinterpret_cast<const double*>(ref),
+                    reinterpret_cast<const double*>(g), list, starts, n, k, d, c0,
+                    reinterpret_cast<double*>(grad_ref));
         }
-        cudaError_t e = cudaMemsetAsync(seg_end, 0, sizeof(int) * size_t(n), s);
-        if (e != cudaSuccess) return fail(TK_ECUDA, std::string("memset: ") + cudaGetErrorString(e));
-        if (np > 0) k_segment_bounds<<<unsigned((np + 255) / 256), 256, 0, s>>>(sk, np, n, seg_start, seg_end);
-        k_grad_ref<T, D><<<(n + bs - 1) / bs, bs, 0, s>>>(q, ref, g, sv, seg_start, seg_end, n, k, d, grad_ref);
     }
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return fail(TK_ECUDA, std::string("backward launch: ") + cudaGetErrorString(e));

@@ -14,10 +14,13 @@
 //      counter (the work queue); every group looks up its query's cloud and
 //      runs the same exact search as the single-cloud kernel with that
 //      cloud's tree and k.
+// Trees of 4-8 dimensions take the same steps with the wide trees' records
+// and search (batch_wide.cuh); all clouds of a batch have one dims.
 #include <algorithm>
 #include <string>
 #include <vector>
 
+#include "batch_wide.cuh"
 #include "kd_query.cuh"
 #include "sort.cuh"
 #include "tk_internal.h"
@@ -52,12 +55,7 @@ struct BatchArgs {
 };
 
 __device__ __forceinline__ int cloud_of(const long long* prefix, int n_clouds, long long qi) {
-    int lo = 0, hi = n_clouds;  // prefix[lo] <= qi < prefix[hi]
-    while (hi - lo > 1) {
-        const int mid = (lo + hi) >> 1;
-        if (prefix[mid] <= qi) lo = mid; else hi = mid;
-    }
-    return lo;
+    return batch_cloud_of(prefix, n_clouds, qi);
 }
 
 template <typename T, int D>
@@ -183,16 +181,31 @@ int batch_bin_levels(int L, long long nq) {
 }
 
 template <typename T>
+void fill_desc(CloudDesc<T>& d, const tk_tree* t) {
+    d.pts = static_cast<const PointRec<T>*>(t->d_pts);
+    d.medians = static_cast<const T*>(t->d_medians);
+    d.leaf_off = t->d_leaf_off;
+    d.boxes = static_cast<const PointRec<T>*>(t->d_boxes);
+}
+
+template <typename T>
+void fill_desc(WideCloudDesc<T>& d, const tk_tree* t) {
+    d.pts = static_cast<const T*>(t->d_pts);
+    d.perm = t->d_perm;
+    d.medians = static_cast<const T*>(t->d_medians);
+    d.leaf_off = t->d_leaf_off;
+    d.boxes = static_cast<const T*>(t->d_boxes);
+}
+
+// Desc: CloudDesc<T> (trees of 1-3 dims) or WideCloudDesc<T> (4-8 dims).
+template <typename T, typename Desc>
 int upload_descs(tk_batch* b, const tk_tree* const* trees, const int64_t* q_counts, const int32_t* ks) {
-    std::vector<CloudDesc<T>> h(b->n_clouds);
+    std::vector<Desc> h(b->n_clouds);
     int bin_base = 0;
     for (int c = 0; c < b->n_clouds; ++c) {
         const tk_tree* t = trees[c];
-        CloudDesc<T>& d = h[c];
-        d.pts = static_cast<const PointRec<T>*>(t->d_pts);
-        d.medians = static_cast<const T*>(t->d_medians);
-        d.leaf_off = t->d_leaf_off;
-        d.boxes = static_cast<const PointRec<T>*>(t->d_boxes);
+        Desc& d = h[c];
+        fill_desc<T>(d, t);
         d.out_off = b->out_off[c];
         d.levels = t->levels;
         d.k = ks[c];
@@ -202,10 +215,10 @@ int upload_descs(tk_batch* b, const tk_tree* const* trees, const int64_t* q_coun
         bin_base += d.bins;
     }
     b->total_bins = bin_base;
-    cudaError_t e = cudaMalloc(&b->d_desc, sizeof(CloudDesc<T>) * h.size());
+    cudaError_t e = cudaMalloc(&b->d_desc, sizeof(Desc) * h.size());
     if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&b->d_prefix), sizeof(long long) * b->q_prefix.size());
     if (e != cudaSuccess) return fail(TK_ENOMEM, std::string("batch allocation: ") + cudaGetErrorString(e));
-    e = cudaMemcpy(b->d_desc, h.data(), sizeof(CloudDesc<T>) * h.size(), cudaMemcpyHostToDevice);
+    e = cudaMemcpy(b->d_desc, h.data(), sizeof(Desc) * h.size(), cudaMemcpyHostToDevice);
     if (e == cudaSuccess)
         e = cudaMemcpy(b->d_prefix, b->q_prefix.data(), sizeof(long long) * b->q_prefix.size(), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) return fail(TK_ECUDA, std::string("batch upload: ") + cudaGetErrorString(e));
@@ -253,6 +266,44 @@ int run_batch(const tk_batch* b, const T* q, T* dists, int32_t* idx, int G, int 
     return TK_OK;
 }
 
+template <typename T>
+int run_batch_wide(const tk_batch* b, const T* q, T* dists, int32_t* idx, int G, char* ws, cudaStream_t s) {
+    const BatchWs w = batch_ws(b);
+    WideBatchArgs<T> a;
+    a.desc = static_cast<const WideCloudDesc<T>*>(b->d_desc);
+    a.q_prefix = b->d_prefix;
+    a.n_clouds = b->n_clouds;
+    a.dims = b->dims;
+    a.q = q;
+    a.total = int(b->total_q);
+    a.out_d = dists;
+    a.out_i = idx;
+    a.work = reinterpret_cast<int*>(ws + w.counter);
+    int* counts = reinterpret_cast<int*>(ws + w.counts);
+    int* bin_of = reinterpret_cast<int*>(ws + w.bin_of);
+    int* pos_of = reinterpret_cast<int*>(ws + w.pos_of);
+    int* order = reinterpret_cast<int*>(ws + w.order);
+    a.order = order;
+    cudaError_t e = cudaMemsetAsync(counts, 0, sizeof(int) * size_t(b->total_bins), s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(a.work, 0, sizeof(int), s);
+    if (e != cudaSuccess) return fail(TK_ECUDA, std::string("memset: ") + cudaGetErrorString(e));
+    const int nb = (a.total + 255) / 256;
+    batch_wide_bin_launch<T>(a, counts, bin_of, pos_of, s);
+    e = exclusive_scan(counts, b->total_bins, ws + w.scan, s);
+    if (e != cudaSuccess) return fail(TK_ECUDA, std::string("batch scan: ") + cudaGetErrorString(e));
+    k_batch_scatter<<<nb, 256, 0, s>>>(a.total, bin_of, pos_of, counts, order);
+    const int W = record_width(b->dims);
+    const void* kfn = batch_wide_kernel<T>(W, G);
+    if (!kfn) return fail(TK_EUNSUPPORTED, "no batched kernel for this record width / lanes");
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, 256, 0) != cudaSuccess || per_sm <= 0) per_sm = 1;
+    int sms = 1;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);
+    const int need = (a.total + 256 / G - 1) / (256 / G);
+    const int grid = std::max(1, std::min(need, per_sm * sms));
+    return batch_wide_launch<T>(a, W, G, grid, s);
+}
+
 }  // namespace
 
 extern "C" {
@@ -268,10 +319,6 @@ int tk_batch_create(const tk_tree* const* trees, int n_trees, const int64_t* q_c
     b->n_clouds = n_trees;
     b->dtype = trees[0] ? trees[0]->dtype : TK_F32;
     b->dims = trees[0] ? trees[0]->dims : 0;
-    if (b->dims > 3) {
-        delete b;
-        return fail(TK_EUNSUPPORTED, "batched queries take trees of 1 to 3 dimensions (query wider trees one by one)");
-    }
     b->device = trees[0] ? trees[0]->device : 0;
     b->q_prefix.assign(n_trees + 1, 0);
     b->out_off.assign(n_trees, 0);
@@ -300,8 +347,13 @@ int tk_batch_create(const tk_tree* const* trees, int n_trees, const int64_t* q_c
     int prev = -1;
     cudaGetDevice(&prev);
     cudaSetDevice(b->device);
-    const int rc = b->dtype == TK_F32 ? upload_descs<float>(b, trees, q_counts, ks)
-                                      : upload_descs<double>(b, trees, q_counts, ks);
+    int rc;
+    if (b->dims <= 3)
+        rc = b->dtype == TK_F32 ? upload_descs<float, CloudDesc<float>>(b, trees, q_counts, ks)
+                                : upload_descs<double, CloudDesc<double>>(b, trees, q_counts, ks);
+    else
+        rc = b->dtype == TK_F32 ? upload_descs<float, WideCloudDesc<float>>(b, trees, q_counts, ks)
+                                : upload_descs<double, WideCloudDesc<double>>(b, trees, q_counts, ks);
     if (prev >= 0) cudaSetDevice(prev);
     if (rc != TK_OK) {
         if (b->d_desc) cudaFree(b->d_desc);
@@ -335,10 +387,17 @@ int tk_batch_query(const tk_batch* b, const void* q, void* dists, int32_t* idx, 
     if (ws_misaligned(workspace)) return fail(TK_EINVAL, "workspace must be 256-byte aligned");
     int G = threads_per_query;
     if (G <= 0) G = b->max_k <= 16 ? 1 : 8;
-    if (G != 1 && G != 8) return fail(TK_EINVAL, "batched queries run 1 or 8 lanes per query");
+    if (G != 1 && G != 8 && G != 32) return fail(TK_EINVAL, "batched queries run 1, 8 or 32 lanes per query");
     if (G == 1 && b->max_k > 16) return fail(TK_EINVAL, "1 lane per query supports k <= 16 in a batch");
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     char* ws = static_cast<char*>(workspace);
+    if (b->dims > 3) {  // trees of 4-8 dims: 1 or 32 lanes per query (the wide kernels' shapes)
+        const int Gw = G == 1 ? 1 : 32;
+        if (b->dtype == TK_F32)
+            return run_batch_wide<float>(b, static_cast<const float*>(q), static_cast<float*>(dists), idx, Gw, ws, s);
+        return run_batch_wide<double>(b, static_cast<const double*>(q), static_cast<double*>(dists), idx, Gw, ws, s);
+    }
+    if (G == 32) G = 8;  // trees of 1-3 dims: 8-lane groups serve every k <= 128
     if (b->dtype == TK_F32) {
         switch (b->dims) {
             case 1: return run_batch<float, 1>(b, static_cast<const float*>(q), static_cast<float*>(dists), idx, G, prune_boxes != 0, ws, s);
