@@ -259,7 +259,7 @@ constexpr int kT5Rows = 128;   // M (queries per block)
 constexpr int kT5Cols = 256;   // N (references per tile)
 constexpr int kT5EpiWarps = 16; // 4 per 32-lane quarter of the accumulator when reading tensor memory
 constexpr int kT5Chunk = 64;    // accumulator columns per phase (16 per column-group warp)
-constexpr int kT5Buf = 64;      // hit buffer per row: one phase's worth of columns
+constexpr int kT5Buf = 48;      // hit buffer per row and tile parity (a redo phase: 32 columns)
 constexpr int kT5BufStride = kT5Buf + 1;  // row stride of the hit buffer (keys), spreads rows over banks
 constexpr int kT5Threads = 32 * (kT5EpiWarps + 1);
 constexpr float kT5PadNorm = 1e30f;
@@ -331,6 +331,13 @@ __device__ __forceinline__ float key_score(unsigned long long key) {
     return __uint_as_float((u & 0x80000000u) ? (u & 0x7FFFFFFFu) : ~u);
 }
 constexpr unsigned long long kScoreSentinel = (0xFF800000ull << 32) | 0xFFFFFFFFull;  // score +inf
+__device__ __forceinline__ uint32_t score_bits(float sc) {
+    const uint32_t u = __float_as_uint(sc);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float bits_score(uint32_t u) {
+    return __uint_as_float((u & 0x80000000u) ? (u & 0x7FFFFFFFu) : ~u);
+}
 
 // A row's over-fetch list of up to 32 * R keys spread over a warp (slot s on
 // lane s % 32, register s / 32; the first 32 R - C slots are padding below
@@ -374,12 +381,27 @@ struct Tc5Shape {
     static constexpr uint32_t B_BYTES = uint32_t(kT5Cols) * KB;
     static constexpr int KSTEPS = KB / 32;
     static constexpr size_t SMEM = size_t(PL) * A_BYTES + 2 * size_t(PL) * B_BYTES +
-                                   size_t(kT5Rows) * kT5BufStride * 8 +  // hit buffer (score keys)
-                                   size_t(kT5Rows) * sizeof(float) +     // row thresholds
-                                   size_t(kT5Rows) * sizeof(int) +       // hit counts
-                                   4 * sizeof(int);                      // overflow / abort flags per tile parity
+                                   2 * size_t(kT5Rows) * kT5BufStride * 8 +  // hit buffers by tile parity
+                                   size_t(kT5Rows) * sizeof(float) +         // row thresholds
+                                   2 * size_t(kT5Rows) * sizeof(int) +       // hit counts by tile parity
+                                   size_t(kT5Rows) * sizeof(uint32_t) +      // sampled threshold per row
+                                   8 * sizeof(int);                          // overflow / abort flags, 4 tiles
+    static_assert(SMEM <= 232448, "shared memory of the select kernel");
 };
 
+// Candidate search of one block: 128 query rows against one slice of the
+// references, C = 2 CH candidates per row.
+//
+// Sampled first threshold.  Before its slice a block runs PS = C / 4 full
+// tiles spread over the slice (a sample); each epilogue thread takes the
+// minimum of its 64 scores of a sample tile (a group of 64 references of its
+// row), and the row's four threads agree on T0 = the maximum over the row's
+// 4 PS group minima.  At least C distinct references of the slice score <= T0
+// (each group's minimum), so the slice's C-th best score is <= T0 and T0 is a
+// valid threshold from the first tile on: the lists start empty, but only
+// references scoring <= T0 enter them, instead of every score of the first
+// tiles.  The sample tiles are scanned again as part of the slice; slices of
+// fewer than 2 PS full tiles skip the sample.
 template <int MODE, int KP, int CH>
 __global__ void __launch_bounds__(kT5Threads, 1) k_tc5_select(const Tc5Args a) {
     using Sh = Tc5Shape<MODE, KP, CH>;
@@ -392,10 +414,11 @@ __global__ void __launch_bounds__(kT5Threads, 1) k_tc5_select(const Tc5Args a) {
     extern __shared__ __align__(1024) unsigned char smem[];
     unsigned char* sA = smem;                       // [PL][A_BYTES]
     unsigned char* sB = smem + PL * A_BYTES;        // [2 stages][PL][B_BYTES]
-    unsigned long long* sBuf = reinterpret_cast<unsigned long long*>(sB + 2 * PL * B_BYTES);  // [kT5Rows][stride]
-    float* sThr = reinterpret_cast<float*>(sBuf + kT5Rows * kT5BufStride);  // [kT5Rows] list threshold per row
-    int* sCnt = reinterpret_cast<int*>(sThr + kT5Rows);                    // [kT5Rows] buffered hits per row
-    int* sFlag = sCnt + kT5Rows;  // [0..1] overflow, [2..3] abort, by tile parity
+    unsigned long long* sBuf = reinterpret_cast<unsigned long long*>(sB + 2 * PL * B_BYTES);  // [2][kT5Rows][stride]
+    float* sThr = reinterpret_cast<float*>(sBuf + 2 * kT5Rows * kT5BufStride);  // [kT5Rows] list threshold per row
+    int* sCnt = reinterpret_cast<int*>(sThr + kT5Rows);                        // [2][kT5Rows] buffered hits per row
+    uint32_t* sT0 = reinterpret_cast<uint32_t*>(sCnt + 2 * kT5Rows);  // [kT5Rows] sampled threshold (bits)
+    int* sFlag = reinterpret_cast<int*>(sT0 + kT5Rows);  // [0..3] overflow, [4..7] abort, by step mod 4
     __shared__ __align__(8) uint64_t full_a, full_b[2], mma_done[2], epi_done[2];
     __shared__ uint32_t tmem_base_sh;
     __shared__ int abort_sh;
@@ -412,6 +435,13 @@ __global__ void __launch_bounds__(kT5Threads, 1) k_tc5_select(const Tc5Args a) {
     const int r1 = int(min((long long)a.n, per * (blockIdx.y + 1)));
     const int ntiles = (r1 - r0 + kT5Cols - 1) / kT5Cols;
     const int tile0 = r0 / kT5Cols;
+    constexpr int PS = (C + 3) / 4;             // sample tiles (4 groups of a row per tile)
+    const int nfull = (r1 - r0) / kT5Cols;
+    const int npre = nfull >= 2 * PS ? PS : 0;  // sample tiles run before the slice
+    const int pstride = npre ? nfull / PS : 1;
+    const int nseq = npre + ntiles;             // tiles through the pipeline
+    // slice tile of pipeline step t: the samples s * pstride, then 0 .. ntiles - 1
+    auto tile_of = [&](int t) { return t < npre ? t * pstride : t - npre; };
 
     if (tid == 0) {
         sm100::mbar_init(&full_a, 1);
@@ -432,7 +462,7 @@ __global__ void __launch_bounds__(kT5Threads, 1) k_tc5_select(const Tc5Args a) {
 
     if (warp == kT5EpiWarps) {
         // ------------------------------------------------ producer / MMA issuer
-        if (lane == 0 && ntiles > 0) {
+        if (lane == 0 && nseq > 0) {
             bool ok = true;
             // what this thread started and has not yet seen complete, per
             // stage: the tile last copied in / waited for, last committed /
@@ -443,15 +473,14 @@ __global__ void __launch_bounds__(kT5Threads, 1) k_tc5_select(const Tc5Args a) {
             sm100::mbar_arrive_expect_tx(&full_a, PL * A_BYTES);
             sm100::bulk_g2s(sA, a.a_hi + (size_t)blockIdx.x * A_BYTES, A_BYTES, &full_a);
             if (PL == 2) sm100::bulk_g2s(sA + A_BYTES, a.a_lo + (size_t)blockIdx.x * A_BYTES, A_BYTES, &full_a);
-            for (int t = 0; t < 2 && t < ntiles; ++t) {
+            for (int t = 0; t < 2 && t < nseq; ++t) {
+                const size_t tb = (size_t)(tile0 + tile_of(t)) * B_BYTES;
                 sm100::mbar_arrive_expect_tx(&full_b[t], PL * B_BYTES);
-                sm100::bulk_g2s(sB + (t * PL) * B_BYTES, a.b_hi + (size_t)(tile0 + t) * B_BYTES, B_BYTES, &full_b[t]);
-                if (PL == 2)
-                    sm100::bulk_g2s(sB + (t * PL + 1) * B_BYTES, a.b_lo + (size_t)(tile0 + t) * B_BYTES, B_BYTES,
-                                    &full_b[t]);
+                sm100::bulk_g2s(sB + (t * PL) * B_BYTES, a.b_hi + tb, B_BYTES, &full_b[t]);
+                if (PL == 2) sm100::bulk_g2s(sB + (t * PL + 1) * B_BYTES, a.b_lo + tb, B_BYTES, &full_b[t]);
                 b_issued[t] = t;
             }
-            for (int t = 0; t < ntiles; ++t) {
+            for (int t = 0; t < nseq; ++t) {
                 const int st = t & 1;
                 const uint32_t ph = (t >> 1) & 1;  // stage st serves tiles st, st + 2, ...: phase t / 2
                 ok = sm100::mbar_wait(&full_b[st], ph, a.max_tries);
@@ -485,16 +514,14 @@ __global__ void __launch_bounds__(kT5Threads, 1) k_tc5_select(const Tc5Args a) {
                 }
                 sm100::mma_commit(&mma_done[st]);
                 m_issued[st] = t;
-                if (t + 2 < ntiles) {
+                if (t + 2 < nseq) {
                     ok = sm100::mbar_wait(&mma_done[st], ph, a.max_tries);  // stage st no longer read
                     if (!ok) break;
                     m_waited[st] = t;
+                    const size_t tb = (size_t)(tile0 + tile_of(t + 2)) * B_BYTES;
                     sm100::mbar_arrive_expect_tx(&full_b[st], PL * B_BYTES);
-                    sm100::bulk_g2s(sB + (st * PL) * B_BYTES, a.b_hi + (size_t)(tile0 + t + 2) * B_BYTES, B_BYTES,
-                                    &full_b[st]);
-                    if (PL == 2)
-                        sm100::bulk_g2s(sB + (st * PL + 1) * B_BYTES, a.b_lo + (size_t)(tile0 + t + 2) * B_BYTES,
-                                        B_BYTES, &full_b[st]);
+                    sm100::bulk_g2s(sB + (st * PL) * B_BYTES, a.b_hi + tb, B_BYTES, &full_b[st]);
+                    if (PL == 2) sm100::bulk_g2s(sB + (st * PL + 1) * B_BYTES, a.b_lo + tb, B_BYTES, &full_b[st]);
                     b_issued[st] = t + 2;
                 }
             }
@@ -522,13 +549,16 @@ __global__ void __launch_bounds__(kT5Threads, 1) k_tc5_select(const Tc5Args a) {
         // query row `myrow`, and the 16-column group w >> 2 of every 64-column
         // phase.  Each score is compared with the row's threshold (the worst
         // key of its over-fetch list, possibly stale but never too small);
-        // the rare hits are appended to the row's buffer in shared memory.
-        // After a tile, warp w merges the buffers of rows 8w .. 8w+7 into
-        // their lists (kept in its registers, one row per group of 4 lanes)
-        // and publishes the new thresholds.  A row can take at most kT5Buf hits per tile on this
-        // path; a tile that overflows a buffer (the first tiles of a slice,
-        // while the lists fill) is done again from tensor memory in four
-        // phases of 64 columns, merging after each, which cannot overflow.
+        // the rare hits are appended to the row's buffer of the tile's parity
+        // in shared memory.  One barrier per tile: after it the tile's
+        // accumulator is released to the MMA issuer, and warp w merges the
+        // buffers of rows 8w .. 8w+7 into their lists (kept in its registers,
+        // one row per group of 4 lanes) while the other warps may already be
+        // filtering the next tile into the other parity's buffers.  A row can
+        // take at most kT5Buf hits per tile on this path; a tile that
+        // overflows a buffer (the first tiles of a slice, while the lists
+        // fill) is done again from tensor memory in eight steps of 32
+        // columns, merging after each, which cannot overflow.
         const int quarter = warp & 3, cgroup = warp >> 2;
         const int myrow = 32 * quarter + lane;
         const int grow = warp * ROWS_PER_WARP + (lane >> 2);  // the row this lane's group keeps
@@ -536,107 +566,146 @@ __global__ void __launch_bounds__(kT5Threads, 1) k_tc5_select(const Tc5Args a) {
         GroupList<RS> glist;
         glist.init();
         unsigned long long gworst = kScoreSentinel;
+        float t0g = __int_as_float(0x7f800000);   // T0 of row grow
+        float tmax = __int_as_float(0xff800000);  // sample: max of this thread's group minima
         const uint32_t trow = tmem + (uint32_t(32 * quarter) << 16);
         constexpr int NPHASE = kT5Cols / kT5Chunk;
         if (tid < kT5Rows) {
             sThr[tid] = __int_as_float(0x7f800000);
             sCnt[tid] = 0;
+            sCnt[kT5Rows + tid] = 0;
+            sT0[tid] = 0u;  // below the image of every score
         }
-        if (tid < 4) sFlag[tid] = 0;
+        if (tid < 8) sFlag[tid] = 0;
         auto bar_epi = [&]() { asm volatile("bar.sync 1, %0;" ::"r"(NEPI) : "memory"); };
         bar_epi();
-        unsigned long long* myBuf = sBuf + myrow * kT5BufStride;
         // compare 16 scores of columns col0 .. col0+15 with thr, append the hits
-        // (`edge`: the columns may run past the slice's end, in its last tile)
-        auto append16 = [&](const float (&v)[16], int col0, float thr, int* ovf, bool edge) {
+        // to buffer parity `par` (`edge`: the columns may run past the slice's
+        // end, in its last tile)
+        auto append16 = [&](const float (&v)[16], int col0, float thr, float pthr, int par, int* ovf, bool edge) {
+            float m = v[0];
+#pragma unroll
+            for (int i = 1; i < 16; ++i) m = fminf(m, v[i]);
+            if (!(m <= pthr)) return;  // no hit among the 16 (pthr = thr once hits are rare)
+            unsigned long long* buf = sBuf + (par * kT5Rows + myrow) * kT5BufStride;
+            int* cnt = sCnt + par * kT5Rows + myrow;
 #pragma unroll
             for (int i = 0; i < 16; ++i) {
                 if (v[i] <= thr && (!edge || col0 + i < r1)) {
-                    const int pos = atomicAdd(&sCnt[myrow], 1);
-                    if (pos < kT5Buf) myBuf[pos] = score_key(v[i], uint32_t(col0 + i));
+                    const int pos = atomicAdd(cnt, 1);
+                    if (pos < kT5Buf) buf[pos] = score_key(v[i], uint32_t(col0 + i));
                     else *ovf = 1;
                 }
             }
         };
-        // merge the buffered hits of this warp's rows into their lists: the 8
-        // rows side by side, one hit of each row per step (a row out of hits
-        // offers the sentinel); a step no row can use is skipped
-        auto merge = [&]() {
-            const int n = min(sCnt[grow], kT5Buf);  // the same on the 4 lanes of a group
-            const unsigned long long* B = sBuf + grow * kT5BufStride;
+        // merge the buffered hits (parity par) of this warp's rows into their
+        // lists: the 8 rows side by side, one hit of each row per step (a row
+        // out of hits offers the sentinel); a step no row can use is skipped
+        auto merge = [&](int par) {
+            int* cnt = sCnt + par * kT5Rows + grow;
+            const int n = min(*cnt, kT5Buf);  // the same on the 4 lanes of a group
+            const unsigned long long* B = sBuf + (par * kT5Rows + grow) * kT5BufStride;
             const int nmax = __reduce_max_sync(0xFFFFFFFFu, n);
+            // the last lane of a group holds the row's worst key: it alone
+            // decides whether its row can use the step (no shuffle per step),
+            // and the next hit is loaded while this one is inserted
+            unsigned long long c = 0 < n ? B[0] : kScoreSentinel;
             for (int h = 0; h < nmax; ++h) {
-                const unsigned long long c = h < n ? B[h] : kScoreSentinel;
-                if (__any_sync(0xFFFFFFFFu, c < gworst)) {
-                    glist.insert(c, gl);
-                    gworst = glist.worst();
-                }
+                const unsigned long long cn = h + 1 < n ? B[h + 1] : kScoreSentinel;
+                if (__any_sync(0xFFFFFFFFu, gl == 3 && c < glist.slot[RS - 1])) glist.insert(c, gl);
+                c = cn;
             }
-            __syncwarp();
+            gworst = glist.worst();
             if (gl == 0 && n > 0) {
-                sCnt[grow] = 0;
-                sThr[grow] = key_score(gworst);
+                *cnt = 0;
+                sThr[grow] = fminf(t0g, key_score(gworst));
             }
         };
-        for (int t = 0; t < ntiles; ++t) {
-            const int st = t & 1, par = t & 1;
+        for (int t = 0; t < nseq; ++t) {
+            const int st = t & 1, par = t & 1, f4 = t & 3;
             const uint32_t ph = (t >> 1) & 1;
-            const int base = r0 + t * kT5Cols;
+            const bool pre = t < npre;
+            const int tt = tile_of(t);
+            const int base = r0 + tt * kT5Cols;
             const uint32_t tcol = trow + uint32_t(st * kT5Cols);
             int w_ok = 1;
             if (lane == 0) w_ok = sm100::mbar_wait(&mma_done[st], ph, a.max_tries);
             w_ok = __shfl_sync(0xFFFFFFFFu, w_ok, 0);
-            if (tid == 0) {  // flags of the next tile (their last readers passed this tile's first barrier)
-                sFlag[par ^ 1] = 0;
-                sFlag[2 + (par ^ 1)] = 0;
+            if (tid == 0) {  // flags of tile t + 2 (their last readers read them before the barrier of tile t - 1)
+                sFlag[(f4 + 2) & 3] = 0;
+                sFlag[4 + ((f4 + 2) & 3)] = 0;
             }
-            if (w_ok) {
+            if (w_ok && pre) {
+                sm100::tc_fence_after();
+                float m = __int_as_float(0x7f800000);
+#pragma unroll 1
+                for (int j = 0; j < NPHASE; ++j) {
+                    float v0[16];
+                    sm100::tmem_ld16(tcol + uint32_t(j * kT5Chunk + cgroup * 16), v0);
+#pragma unroll
+                    for (int i = 0; i < 16; ++i) m = fminf(m, v0[i]);
+                }
+                tmax = fmaxf(tmax, m);
+            } else if (w_ok) {
                 sm100::tc_fence_after();
                 const float thr = sThr[myrow];
+                // the 16-score pre-check pays once hits are rare (from the 16th tile of the slice on)
+                const float pthr = tt >= 16 ? thr : __int_as_float(0x7f800000);
                 const bool edge = base + kT5Cols > r1;
 #pragma unroll
                 for (int j = 0; j < NPHASE; j += 2) {
                     float v0[16], v1[16];
                     sm100::tmem_ld16x2(tcol + uint32_t(j * kT5Chunk + cgroup * 16),
                                        tcol + uint32_t((j + 1) * kT5Chunk + cgroup * 16), v0, v1);
-                    append16(v0, base + j * kT5Chunk + cgroup * 16, thr, &sFlag[par], edge);
-                    append16(v1, base + (j + 1) * kT5Chunk + cgroup * 16, thr, &sFlag[par], edge);
+                    append16(v0, base + j * kT5Chunk + cgroup * 16, thr, pthr, par, &sFlag[f4], edge);
+                    append16(v1, base + (j + 1) * kT5Chunk + cgroup * 16, thr, pthr, par, &sFlag[f4], edge);
                 }
             } else if (lane == 0) {
-                sFlag[2 + par] = 1;
+                sFlag[4 + f4] = 1;
             }
             bar_epi();
-            const int bad = sFlag[2 + par];   // agreed: written only before the barrier above
-            const int ovf = sFlag[par];
-            if (!bad) {
-                if (!ovf) {
-                    merge();
-                } else {
-                    // redo the tile in four phases of 64 columns
-                    if (tid < kT5Rows) sCnt[tid] = 0;
-                    bar_epi();
+            const int bad = sFlag[4 + f4];   // agreed: written only before the barrier above
+            const int ovf = sFlag[f4];
+            if (!bad && pre && t == npre - 1) {
+                // the row's four threads agree on T0 = max of the row's group minima
+                if (tmax == tmax) atomicMax(&sT0[myrow], score_bits(tmax));
+                bar_epi();
+                if (tid < kT5Rows) {
+                    const uint32_t u = sT0[tid];
+                    sThr[tid] = u ? bits_score(u) : __int_as_float(0x7f800000);
+                }
+                const uint32_t u = sT0[grow];
+                t0g = u ? bits_score(u) : __int_as_float(0x7f800000);
+                bar_epi();
+            }
+            if (!bad && ovf) {
+                // redo the tile in eight steps of 32 columns (two column groups each)
+                if (tid < kT5Rows) sCnt[par * kT5Rows + tid] = 0;
+                bar_epi();
 #pragma unroll 1
-                    for (int j = 0; j < NPHASE; ++j) {
+                for (int j = 0; j < 2 * NPHASE; ++j) {
+                    if ((cgroup >> 1) == (j & 1)) {
                         const float thr = sThr[myrow];
                         float v[16];
-                        sm100::tmem_ld16(tcol + uint32_t(j * kT5Chunk + cgroup * 16), v);
+                        sm100::tmem_ld16(tcol + uint32_t((j >> 1) * kT5Chunk + cgroup * 16), v);
                         int dummy = 0;
-                        append16(v, base + j * kT5Chunk + cgroup * 16, thr, &dummy, true);  // <= 64 hits per row
-                        bar_epi();
-                        merge();
-                        bar_epi();
+                        append16(v, base + (j >> 1) * kT5Chunk + cgroup * 16, thr, __int_as_float(0x7f800000), par,
+                                 &dummy, true);  // <= 32 hits per row
                     }
+                    bar_epi();
+                    merge(par);
+                    bar_epi();
                 }
             }
             // this tile's accumulator is no longer read
             sm100::tc_fence_before();
             __syncwarp();
             if (lane == 0) sm100::mbar_arrive(&epi_done[st]);
-            bar_epi();
             if (bad) {
                 if (tid == 0) atomicOr(a.err, kTcErrTimeout);
                 break;
             }
+            if (!ovf && !pre) merge(par);
         }
         // write the lists: C candidates per row and the row threshold
         {
