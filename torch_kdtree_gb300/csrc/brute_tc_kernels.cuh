@@ -261,6 +261,7 @@ constexpr int kT5EpiWarps = 16; // 4 per 32-lane quarter of the accumulator when
 constexpr int kT5Chunk = 64;    // accumulator columns per phase (16 per column-group warp)
 constexpr int kT5Buf = 48;      // hit buffer per row and tile parity (a redo phase: 32 columns)
 constexpr int kT5BufStride = kT5Buf + 1;  // row stride of the hit buffer (keys), spreads rows over banks
+constexpr int kT5MinStride = 129;         // row stride (words) of the sample's group minima: 2C <= 128
 constexpr int kT5Threads = 32 * (kT5EpiWarps + 1);
 constexpr float kT5PadNorm = 1e30f;
 constexpr uint32_t kT5MaxTries = 1u << 22;  // bounded mbarrier polls (default; Tc5Args::max_tries)
@@ -384,9 +385,10 @@ struct Tc5Shape {
                                    2 * size_t(kT5Rows) * kT5BufStride * 8 +  // hit buffers by tile parity
                                    size_t(kT5Rows) * sizeof(float) +         // row thresholds
                                    2 * size_t(kT5Rows) * sizeof(int) +       // hit counts by tile parity
-                                   size_t(kT5Rows) * sizeof(uint32_t) +      // sampled threshold per row
                                    8 * sizeof(int);                          // overflow / abort flags, 4 tiles
     static_assert(SMEM <= 232448, "shared memory of the select kernel");
+    static_assert(size_t(kT5Rows) * kT5MinStride * 4 <= 2 * size_t(kT5Rows) * kT5BufStride * 8 && 4 * CH <= 128,
+                  "the sample's minima fit the hit buffers");
 };
 
 // Candidate search of one block: 128 query rows against one slice of the
@@ -394,14 +396,17 @@ struct Tc5Shape {
 //
 // Sampled first threshold.  Before its slice a block runs PS = C / 4 full
 // tiles spread over the slice (a sample); each epilogue thread takes the
-// minimum of its 64 scores of a sample tile (a group of 64 references of its
-// row), and the row's four threads agree on T0 = the maximum over the row's
-// 4 PS group minima.  At least C distinct references of the slice score <= T0
-// (each group's minimum), so the slice's C-th best score is <= T0 and T0 is a
+// minima of the two halves of its 64 scores of a sample tile (two groups of 32
+// references of its row), and the row's four list lanes find T0 = the C-th
+// smallest of the row's 2C group minima (bisection on their order-preserving
+// images).  At least C distinct references of the slice score <= T0 (the
+// minima of C groups), so the slice's C-th best score is <= T0 and T0 is a
 // valid threshold from the first tile on: the lists start empty, but only
 // references scoring <= T0 enter them, instead of every score of the first
-// tiles.  The sample tiles are scanned again as part of the slice; slices of
-// fewer than 2 PS full tiles skip the sample.
+// tiles.  (The C-th of 2C minima of 32 scores sits near the 2% quantile of a
+// row's scores; the maximum of C minima of 64, tried first, near 7%.)  The
+// sample tiles are scanned again as part of the slice; slices of fewer than
+// 2 PS full tiles skip the sample.
 template <int MODE, int KP, int CH>
 __global__ void __launch_bounds__(kT5Threads, 1) k_tc5_select(const Tc5Args a) {
     using Sh = Tc5Shape<MODE, KP, CH>;
@@ -417,8 +422,7 @@ __global__ void __launch_bounds__(kT5Threads, 1) k_tc5_select(const Tc5Args a) {
     unsigned long long* sBuf = reinterpret_cast<unsigned long long*>(sB + 2 * PL * B_BYTES);  // [2][kT5Rows][stride]
     float* sThr = reinterpret_cast<float*>(sBuf + 2 * kT5Rows * kT5BufStride);  // [kT5Rows] list threshold per row
     int* sCnt = reinterpret_cast<int*>(sThr + kT5Rows);                        // [2][kT5Rows] buffered hits per row
-    uint32_t* sT0 = reinterpret_cast<uint32_t*>(sCnt + 2 * kT5Rows);  // [kT5Rows] sampled threshold (bits)
-    int* sFlag = reinterpret_cast<int*>(sT0 + kT5Rows);  // [0..3] overflow, [4..7] abort, by step mod 4
+    int* sFlag = sCnt + 2 * kT5Rows;  // [0..3] overflow, [4..7] abort, by step mod 4
     __shared__ __align__(8) uint64_t full_a, full_b[2], mma_done[2], epi_done[2];
     __shared__ uint32_t tmem_base_sh;
     __shared__ int abort_sh;
@@ -567,14 +571,14 @@ __global__ void __launch_bounds__(kT5Threads, 1) k_tc5_select(const Tc5Args a) {
         glist.init();
         unsigned long long gworst = kScoreSentinel;
         float t0g = __int_as_float(0x7f800000);   // T0 of row grow
-        float tmax = __int_as_float(0xff800000);  // sample: max of this thread's group minima
+        // the sample's group minima (images), 2C per row, in the hit buffers' space
+        uint32_t* sMin = reinterpret_cast<uint32_t*>(sBuf);
         const uint32_t trow = tmem + (uint32_t(32 * quarter) << 16);
         constexpr int NPHASE = kT5Cols / kT5Chunk;
         if (tid < kT5Rows) {
             sThr[tid] = __int_as_float(0x7f800000);
             sCnt[tid] = 0;
             sCnt[kT5Rows + tid] = 0;
-            sT0[tid] = 0u;  // below the image of every score
         }
         if (tid < 8) sFlag[tid] = 0;
         auto bar_epi = [&]() { asm volatile("bar.sync 1, %0;" ::"r"(NEPI) : "memory"); };
@@ -636,16 +640,20 @@ __global__ void __launch_bounds__(kT5Threads, 1) k_tc5_select(const Tc5Args a) {
                 sFlag[4 + ((f4 + 2) & 3)] = 0;
             }
             if (w_ok && pre) {
+                // two group minima (32 scores each) of this thread's row per sample tile
                 sm100::tc_fence_after();
-                float m = __int_as_float(0x7f800000);
 #pragma unroll 1
-                for (int j = 0; j < NPHASE; ++j) {
-                    float v0[16];
-                    sm100::tmem_ld16(tcol + uint32_t(j * kT5Chunk + cgroup * 16), v0);
+                for (int h = 0; h < 2; ++h) {
+                    float m = __int_as_float(0x7f800000);
+#pragma unroll 1
+                    for (int j = 2 * h; j < 2 * h + 2; ++j) {
+                        float v0[16];
+                        sm100::tmem_ld16(tcol + uint32_t(j * kT5Chunk + cgroup * 16), v0);
 #pragma unroll
-                    for (int i = 0; i < 16; ++i) m = fminf(m, v0[i]);
+                        for (int i = 0; i < 16; ++i) m = fminf(m, v0[i]);
+                    }
+                    sMin[myrow * kT5MinStride + t * 8 + cgroup * 2 + h] = m == m ? score_bits(m) : 0xFFFFFFFFu;
                 }
-                tmax = fmaxf(tmax, m);
             } else if (w_ok) {
                 sm100::tc_fence_after();
                 const float thr = sThr[myrow];
@@ -667,16 +675,27 @@ __global__ void __launch_bounds__(kT5Threads, 1) k_tc5_select(const Tc5Args a) {
             const int bad = sFlag[4 + f4];   // agreed: written only before the barrier above
             const int ovf = sFlag[f4];
             if (!bad && pre && t == npre - 1) {
-                // the row's four threads agree on T0 = max of the row's group minima
-                if (tmax == tmax) atomicMax(&sT0[myrow], score_bits(tmax));
-                bar_epi();
-                if (tid < kT5Rows) {
-                    const uint32_t u = sT0[tid];
-                    sThr[tid] = u ? bits_score(u) : __int_as_float(0x7f800000);
+                // T0 of row grow = the C-th smallest of its 2C group minima,
+                // found by the row's 4 lanes by bisection on the order-
+                // preserving image (C/2 minima per lane, interleaved so that
+                // the 4 lanes read 4 different banks)
+                const uint32_t* mins = sMin + grow * kT5MinStride + gl;
+                uint32_t lo = 0u, hi = 0xFFFFFFFFu;
+#pragma unroll 1
+                for (int it = 0; it < 32; ++it) {
+                    const uint32_t mid = lo + ((hi - lo) >> 1);
+                    int cnt = 0;
+#pragma unroll 8
+                    for (int i = 0; i < C / 2; ++i) cnt += mins[4 * i] <= mid ? 1 : 0;
+                    cnt += __shfl_xor_sync(0xFFFFFFFFu, cnt, 1);
+                    cnt += __shfl_xor_sync(0xFFFFFFFFu, cnt, 2);
+                    if (cnt >= C) hi = mid;
+                    else lo = mid + 1u;
                 }
-                const uint32_t u = sT0[grow];
-                t0g = u ? bits_score(u) : __int_as_float(0x7f800000);
-                bar_epi();
+                // images above +inf's are NaN minima (never certified): no threshold
+                t0g = lo < 0xFF800000u ? bits_score(lo) : __int_as_float(0x7f800000);
+                if (gl == 0) sThr[grow] = t0g;
+                bar_epi();  // the sample's minima (in the hit buffers) are no longer read
             }
             if (!bad && ovf) {
                 // redo the tile in eight steps of 32 columns (two column groups each)
