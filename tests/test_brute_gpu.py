@@ -123,6 +123,32 @@ def test_tensor_core_modes_are_exact(mode, d, k, oracle):
 
 
 @pytest.mark.parametrize("mode", ["tf32", "bf16_split"])
+@pytest.mark.parametrize("k", [8, 32])
+@pytest.mark.parametrize("data", ["normal", "repeated", "grid"])
+def test_tensor_core_sampled_threshold_slices(mode, k, data, oracle):
+    """Slices long enough (70,000 refs, 8 slices of ~34 tiles) that the
+    candidate kernel first samples a threshold: on N(0,1) data, on 300
+    distinct points repeated (every tile overflows the hit buffers and is
+    redone in 32-column steps) and on an integer grid (exact distance ties).
+    The answer must stay the exhaustive search's, bit for bit."""
+    rng = np.random.default_rng(4100 + k)
+    d = 16
+    if data == "normal":
+        ref = rng.standard_normal((70000, d)).astype(np.float32)
+    elif data == "repeated":
+        ref = rng.standard_normal((300, d)).astype(np.float32)[rng.integers(0, 300, 70000)]
+    else:
+        ref = rng.integers(-3, 4, (70000, d)).astype(np.float32)
+    q = rng.standard_normal((600, d)).astype(np.float32)
+    if data == "grid":
+        q = np.rint(q)  # integer distances: many exact ties
+    dd, ii = tk().nn_distance(torch.from_numpy(ref).to(cuda), torch.from_numpy(q).to(cuda), k, mode=mode)
+    bd, bi = oracle.brute(ref, q, k)
+    np.testing.assert_array_equal(dd.cpu().numpy(), bd)
+    np.testing.assert_array_equal(ii.cpu().numpy(), bi)
+
+
+@pytest.mark.parametrize("mode", ["tf32", "bf16_split"])
 def test_tensor_core_fallback_on_massive_ties(mode, oracle):
     """64 distinct points repeated ~300 times: candidate lists cannot separate
     the k-th neighbour from the rest, the certificate fails and the exact
