@@ -123,7 +123,7 @@ def test_tensor_core_modes_are_exact(mode, d, k, oracle):
 
 
 @pytest.mark.parametrize("mode", ["tf32", "bf16_split"])
-@pytest.mark.parametrize("k", [8, 32])
+@pytest.mark.parametrize("k", [8, 16, 32])
 @pytest.mark.parametrize("data", ["normal", "repeated", "grid"])
 def test_tensor_core_sampled_threshold_slices(mode, k, data, oracle):
     """Slices long enough (70,000 refs, 8 slices of ~34 tiles) that the
