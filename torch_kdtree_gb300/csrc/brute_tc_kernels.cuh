@@ -394,17 +394,18 @@ struct Tc5Shape {
 // Candidate search of one block: 128 query rows against one slice of the
 // references, C = 2 CH candidates per row.
 //
-// Sampled first threshold.  Before its slice a block runs PS = C / 4 full
+// Sampled first threshold.  Before its slice a block runs PS = C / 2 full
 // tiles spread over the slice (a sample); each epilogue thread takes the
-// minima of the two halves of its 64 scores of a sample tile (two groups of 32
-// references of its row), and the row's four list lanes find T0 = the C-th
-// smallest of the row's 2C group minima (bisection on their order-preserving
-// images).  At least C distinct references of the slice score <= T0 (the
-// minima of C groups), so the slice's C-th best score is <= T0 and T0 is a
-// valid threshold from the first tile on: the lists start empty, but only
+// minimum of its 64 scores of a sample tile (a group of 64 references of its
+// row), and the row's four list lanes find T0 = the C-th smallest of the
+// row's 2C group minima (bisection on their order-preserving images).  At
+// least C distinct references of the slice score <= T0 (the minima of C
+// groups), so the slice's C-th best score is <= T0 and T0 is a valid
+// threshold from the first tile on: the lists start empty, but only
 // references scoring <= T0 enter them, instead of every score of the first
-// tiles.  (The C-th of 2C minima of 32 scores sits near the 2% quantile of a
-// row's scores; the maximum of C minima of 64, tried first, near 7%.)  The
+// tiles.  (The C-th of 2C minima of 64 scores sits near the 1% quantile of a
+// row's scores; C / 4 sample tiles with minima of 32 scores, near 2%, were
+// 2-5% slower, and the maximum of C minima, near 7%, slower still.)  The
 // sample tiles are scanned again as part of the slice; slices of fewer than
 // 2 PS full tiles skip the sample.
 template <int MODE, int KP, int CH>
@@ -439,7 +440,7 @@ __global__ void __launch_bounds__(kT5Threads, 1) k_tc5_select(const Tc5Args a) {
     const int r1 = int(min((long long)a.n, per * (blockIdx.y + 1)));
     const int ntiles = (r1 - r0 + kT5Cols - 1) / kT5Cols;
     const int tile0 = r0 / kT5Cols;
-    constexpr int PS = (C + 3) / 4;             // sample tiles (4 groups of a row per tile)
+    constexpr int PS = (C + 1) / 2;             // sample tiles (4 group minima of a row per tile)
     const int nfull = (r1 - r0) / kT5Cols;
     const int npre = nfull >= 2 * PS ? PS : 0;  // sample tiles run before the slice
     const int pstride = npre ? nfull / PS : 1;
@@ -640,20 +641,17 @@ __global__ void __launch_bounds__(kT5Threads, 1) k_tc5_select(const Tc5Args a) {
                 sFlag[4 + ((f4 + 2) & 3)] = 0;
             }
             if (w_ok && pre) {
-                // two group minima (32 scores each) of this thread's row per sample tile
+                // one group minimum (64 scores) of this thread's row per sample tile
                 sm100::tc_fence_after();
+                float m = __int_as_float(0x7f800000);
 #pragma unroll 1
-                for (int h = 0; h < 2; ++h) {
-                    float m = __int_as_float(0x7f800000);
-#pragma unroll 1
-                    for (int j = 2 * h; j < 2 * h + 2; ++j) {
-                        float v0[16];
-                        sm100::tmem_ld16(tcol + uint32_t(j * kT5Chunk + cgroup * 16), v0);
+                for (int j = 0; j < NPHASE; ++j) {
+                    float v0[16];
+                    sm100::tmem_ld16(tcol + uint32_t(j * kT5Chunk + cgroup * 16), v0);
 #pragma unroll
-                        for (int i = 0; i < 16; ++i) m = fminf(m, v0[i]);
-                    }
-                    sMin[myrow * kT5MinStride + t * 8 + cgroup * 2 + h] = m == m ? score_bits(m) : 0xFFFFFFFFu;
+                    for (int i = 0; i < 16; ++i) m = fminf(m, v0[i]);
                 }
+                sMin[myrow * kT5MinStride + t * 4 + cgroup] = m == m ? score_bits(m) : 0xFFFFFFFFu;
             } else if (w_ok) {
                 sm100::tc_fence_after();
                 const float thr = sThr[myrow];
