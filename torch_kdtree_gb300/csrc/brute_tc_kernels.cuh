@@ -261,7 +261,10 @@ constexpr int kT5EpiWarps = 16; // 4 per 32-lane quarter of the accumulator when
 constexpr int kT5Chunk = 64;    // accumulator columns per phase (16 per column-group warp)
 constexpr int kT5Buf = 48;      // hit buffer per row and tile parity (a redo phase: 32 columns)
 constexpr int kT5BufStride = kT5Buf + 1;  // row stride of the hit buffer (keys), spreads rows over banks
-constexpr int kT5MinStride = 129;         // row stride (words) of the sample's group minima: 2C <= 128
+// Row stride (words) of the sample's group minima (2C <= 128 per row); 132 = 4
+// mod 32 puts the 32 lanes of a bisection read (8 rows x 4 interleaved lanes)
+// on 32 different banks.
+constexpr int kT5MinStride = 132;
 constexpr int kT5Threads = 32 * (kT5EpiWarps + 1);
 constexpr float kT5PadNorm = 1e30f;
 constexpr uint32_t kT5MaxTries = 1u << 22;  // bounded mbarrier polls (default; Tc5Args::max_tries)
