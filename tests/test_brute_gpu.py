@@ -149,6 +149,25 @@ def test_tensor_core_sampled_threshold_slices(mode, k, data, oracle):
 
 
 @pytest.mark.parametrize("mode", ["tf32", "bf16_split"])
+@pytest.mark.parametrize("n", [1, 7, 255, 256, 257, 513])
+@pytest.mark.parametrize("nq", [1, 5, 129])
+def test_tensor_core_edge_sizes(mode, n, nq, oracle):
+    """Single, partial and exactly-full 256-reference tiles, query blocks of
+    1, 5 and 129 rows (one row past a 128-row block), k up to 32 and at most
+    n: slices far too short for the sampled threshold, the last tile's
+    column bound, padding rows of both operands."""
+    rng = np.random.default_rng(7000 + n + nq)
+    d = 12
+    ref = rng.standard_normal((n, d)).astype(np.float32)
+    q = rng.standard_normal((nq, d)).astype(np.float32)
+    for k in sorted({1, min(n, 5), min(n, 32)}):
+        dd, ii = tk().nn_distance(torch.from_numpy(ref).to(cuda), torch.from_numpy(q).to(cuda), k, mode=mode)
+        bd, bi = oracle.brute(ref, q, k)
+        np.testing.assert_array_equal(dd.cpu().numpy(), bd)
+        np.testing.assert_array_equal(ii.cpu().numpy(), bi)
+
+
+@pytest.mark.parametrize("mode", ["tf32", "bf16_split"])
 def test_tensor_core_fallback_on_massive_ties(mode, oracle):
     """64 distinct points repeated ~300 times: candidate lists cannot separate
     the k-th neighbour from the rest, the certificate fails and the exact
