@@ -388,7 +388,7 @@ struct Tc5Shape {
                                    2 * size_t(kT5Rows) * kT5BufStride * 8 +  // hit buffers by tile parity
                                    size_t(kT5Rows) * sizeof(float) +         // row thresholds
                                    2 * size_t(kT5Rows) * sizeof(int) +       // hit counts by tile parity
-                                   8 * sizeof(int);                          // overflow / abort flags, 4 tiles
+                                   40 * sizeof(int);                         // overflow / abort flags: block, per quarter
     static_assert(SMEM <= 232448, "shared memory of the select kernel");
     static_assert(size_t(kT5Rows) * kT5MinStride * 4 <= 2 * size_t(kT5Rows) * kT5BufStride * 8 && 4 * CH <= 128,
                   "the sample's minima fit the hit buffers");
@@ -426,7 +426,9 @@ __global__ void __launch_bounds__(kT5Threads, 1) k_tc5_select(const Tc5Args a) {
     unsigned long long* sBuf = reinterpret_cast<unsigned long long*>(sB + 2 * PL * B_BYTES);  // [2][kT5Rows][stride]
     float* sThr = reinterpret_cast<float*>(sBuf + 2 * kT5Rows * kT5BufStride);  // [kT5Rows] list threshold per row
     int* sCnt = reinterpret_cast<int*>(sThr + kT5Rows);                        // [2][kT5Rows] buffered hits per row
-    int* sFlag = sCnt + 2 * kT5Rows;  // [0..3] overflow, [4..7] abort, by step mod 4
+    // [0..7] the sample steps' flags (block-wide), then per quarter [8 + 8q ..]:
+    // [0..3] overflow, [4..7] abort, by step mod 4
+    int* sFlag = sCnt + 2 * kT5Rows;
     __shared__ __align__(8) uint64_t full_a, full_b[2], mma_done[2], epi_done[2];
     __shared__ uint32_t tmem_base_sh;
     __shared__ int abort_sh;
@@ -558,18 +560,21 @@ __global__ void __launch_bounds__(kT5Threads, 1) k_tc5_select(const Tc5Args a) {
         // phase.  Each score is compared with the row's threshold (the worst
         // key of its over-fetch list, possibly stale but never too small);
         // the rare hits are appended to the row's buffer of the tile's parity
-        // in shared memory.  One barrier per tile: after it the tile's
-        // accumulator is released to the MMA issuer, and warp w merges the
-        // buffers of rows 8w .. 8w+7 into their lists (kept in its registers,
-        // one row per group of 4 lanes) while the other warps may already be
-        // filtering the next tile into the other parity's buffers.  A row can
+        // in shared memory.  One barrier per tile and accumulator quarter:
+        // after it the tile's accumulator is released to the MMA issuer, and
+        // warp w merges the buffers of its quarter's rows 32 (w & 3) +
+        // 8 (w >> 2) .. + 7 into their lists (kept in its registers, one row
+        // per group of 4 lanes) while other warps may already be filtering
+        // the next tile into the other parity's buffers.  A row can
         // take at most kT5Buf hits per tile on this path; a tile that
         // overflows a buffer (the first tiles of a slice, while the lists
         // fill) is done again from tensor memory in eight steps of 32
         // columns, merging after each, which cannot overflow.
         const int quarter = warp & 3, cgroup = warp >> 2;
         const int myrow = 32 * quarter + lane;
-        const int grow = warp * ROWS_PER_WARP + (lane >> 2);  // the row this lane's group keeps
+        // the row this lane's group keeps: the 4 warps of a quarter keep its 32 rows
+        const int grow = 32 * quarter + ROWS_PER_WARP * cgroup + (lane >> 2);
+        int* qFlag = sFlag + 8 + 8 * quarter;
         const int gl = lane & 3;
         GroupList<RS> glist;
         glist.init();
@@ -584,9 +589,15 @@ __global__ void __launch_bounds__(kT5Threads, 1) k_tc5_select(const Tc5Args a) {
             sCnt[tid] = 0;
             sCnt[kT5Rows + tid] = 0;
         }
-        if (tid < 8) sFlag[tid] = 0;
-        auto bar_epi = [&]() { asm volatile("bar.sync 1, %0;" ::"r"(NEPI) : "memory"); };
-        bar_epi();
+        if (tid < 40) sFlag[tid] = 0;
+        // The sample steps synchronise all epilogue warps (their minima share
+        // the hit buffers' space across quarters); from the first tile of the
+        // slice on, each quarter (its 4 warps filter and keep the same 32
+        // rows) synchronises on its own named barrier, and the quarters meet
+        // only through the accumulator stages (epi_done).
+        auto bar_all = [&]() { asm volatile("bar.sync 1, %0;" ::"r"(NEPI) : "memory"); };
+        auto bar_quarter = [&]() { asm volatile("bar.sync %0, 128;" ::"r"(2 + quarter) : "memory"); };
+        bar_all();
         // compare 16 scores of columns col0 .. col0+15 with thr, append the hits
         // to buffer parity `par` (`edge`: the columns may run past the slice's
         // end, in its last tile)
@@ -639,9 +650,11 @@ __global__ void __launch_bounds__(kT5Threads, 1) k_tc5_select(const Tc5Args a) {
             int w_ok = 1;
             if (lane == 0) w_ok = sm100::mbar_wait(&mma_done[st], ph, a.max_tries);
             w_ok = __shfl_sync(0xFFFFFFFFu, w_ok, 0);
-            if (tid == 0) {  // flags of tile t + 2 (their last readers read them before the barrier of tile t - 1)
-                sFlag[(f4 + 2) & 3] = 0;
-                sFlag[4 + ((f4 + 2) & 3)] = 0;
+            int* F = pre ? sFlag : qFlag;  // this step's flags (block-wide while sampling)
+            if (pre ? tid == 0 : (cgroup == 0 && lane == 0)) {
+                // flags of step t + 2 (last read before the barrier of step t - 1)
+                F[(f4 + 2) & 3] = 0;
+                F[4 + ((f4 + 2) & 3)] = 0;
             }
             if (w_ok && pre) {
                 // one group minimum (64 scores) of this thread's row per sample tile
@@ -666,15 +679,16 @@ __global__ void __launch_bounds__(kT5Threads, 1) k_tc5_select(const Tc5Args a) {
                     float v0[16], v1[16];
                     sm100::tmem_ld16x2(tcol + uint32_t(j * kT5Chunk + cgroup * 16),
                                        tcol + uint32_t((j + 1) * kT5Chunk + cgroup * 16), v0, v1);
-                    append16(v0, base + j * kT5Chunk + cgroup * 16, thr, pthr, par, &sFlag[f4], edge);
-                    append16(v1, base + (j + 1) * kT5Chunk + cgroup * 16, thr, pthr, par, &sFlag[f4], edge);
+                    append16(v0, base + j * kT5Chunk + cgroup * 16, thr, pthr, par, &F[f4], edge);
+                    append16(v1, base + (j + 1) * kT5Chunk + cgroup * 16, thr, pthr, par, &F[f4], edge);
                 }
             } else if (lane == 0) {
-                sFlag[4 + f4] = 1;
+                F[4 + f4] = 1;
             }
-            bar_epi();
-            const int bad = sFlag[4 + f4];   // agreed: written only before the barrier above
-            const int ovf = sFlag[f4];
+            if (pre) bar_all();
+            else bar_quarter();
+            const int bad = F[4 + f4];   // agreed (block / quarter): written only before the barrier above
+            const int ovf = F[f4];
             if (!bad && pre && t == npre - 1) {
                 // T0 of row grow = the C-th smallest of its 2C group minima,
                 // found by the row's 4 lanes by bisection on the order-
@@ -696,12 +710,12 @@ __global__ void __launch_bounds__(kT5Threads, 1) k_tc5_select(const Tc5Args a) {
                 // images above +inf's are NaN minima (never certified): no threshold
                 t0g = lo < 0xFF800000u ? bits_score(lo) : __int_as_float(0x7f800000);
                 if (gl == 0) sThr[grow] = t0g;
-                bar_epi();  // the sample's minima (in the hit buffers) are no longer read
+                bar_all();  // no quarter appends hits over the sample's minima before all have read them
             }
             if (!bad && ovf) {
                 // redo the tile in eight steps of 32 columns (two column groups each)
-                if (tid < kT5Rows) sCnt[par * kT5Rows + tid] = 0;
-                bar_epi();
+                if (cgroup == 0) sCnt[par * kT5Rows + myrow] = 0;  // the quarter's rows
+                bar_quarter();
 #pragma unroll 1
                 for (int j = 0; j < 2 * NPHASE; ++j) {
                     if ((cgroup >> 1) == (j & 1)) {
@@ -712,9 +726,9 @@ __global__ void __launch_bounds__(kT5Threads, 1) k_tc5_select(const Tc5Args a) {
                         append16(v, base + (j >> 1) * kT5Chunk + cgroup * 16, thr, __int_as_float(0x7f800000), par,
                                  &dummy, true);  // <= 32 hits per row
                     }
-                    bar_epi();
+                    bar_quarter();
                     merge(par);
-                    bar_epi();
+                    bar_quarter();
                 }
             }
             // this tile's accumulator is no longer read
@@ -722,7 +736,7 @@ __global__ void __launch_bounds__(kT5Threads, 1) k_tc5_select(const Tc5Args a) {
             __syncwarp();
             if (lane == 0) sm100::mbar_arrive(&epi_done[st]);
             if (bad) {
-                if (tid == 0) atomicOr(a.err, kTcErrTimeout);
+                if (cgroup == 0 && lane == 0) atomicOr(a.err, kTcErrTimeout);
                 break;
             }
             if (!ovf && !pre) merge(par);
