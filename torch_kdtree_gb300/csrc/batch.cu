@@ -89,9 +89,12 @@ __device__ __forceinline__ void batch_search(const CloudDesc<T>& cd, const T (&q
 }
 
 // G = 1: k <= 16 (registers per lane R in {1, 4, 16});
-// G = 8: k <= 128 (R in {2, 4, 8, 16}).
+// G = 8: k <= 128 (R in {2, 4, 8, 16}).  Capped at 4 blocks of 256 per SM (64
+// registers for float): left free the float kernels took 72-80 registers, 3
+// blocks per SM, and ran the 256 ragged clouds 9-14% slower (a few bytes of
+// spills cost less than a quarter of the resident warps).
 template <typename T, int D, int G>
-__global__ void __launch_bounds__(256) k_batch_query(const BatchArgs<T> a) {
+__global__ void __launch_bounds__(256, 4) k_batch_query(const BatchArgs<T> a) {
     const int lane = threadIdx.x & 31;
     const int gl = lane & (G - 1);
     const int gbase = lane & ~(G - 1);
