@@ -84,7 +84,7 @@ __device__ __forceinline__ void batch_search_wide(const WideCloudDesc<T>& cd, in
 
 // G = 1: k <= 16 (R in {1, 4, 16}); G = 32: k <= 128 (R in {1, 2, 4}).
 template <typename T, int W, int G>
-__global__ void __launch_bounds__(256) k_batch_query_wide(const WideBatchArgs<T> a) {
+__device__ __forceinline__ void batch_query_wide(const WideBatchArgs<T>& a) {
     const int lane = threadIdx.x & 31;
     const int gl = lane & (G - 1);
     const int gbase = lane & ~(G - 1);
@@ -119,6 +119,20 @@ __global__ void __launch_bounds__(256) k_batch_query_wide(const WideBatchArgs<T>
         }
         __syncwarp();
     }
+}
+
+// One lane per query: registers left to the compiler.
+template <typename T, int W>
+__global__ void __launch_bounds__(256) k_batch_query_wide1(const WideBatchArgs<T> a) {
+    batch_query_wide<T, W, 1>(a);
+}
+
+// 32 lanes per query, capped at 4 blocks of 256 per SM (64 registers for
+// float): left free they took 80-117 registers and ran 64 clouds of 4 / 6 / 8
+// dims 14% / 7% / 32% slower.
+template <typename T, int W>
+__global__ void __launch_bounds__(256, 4) k_batch_query_wide32(const WideBatchArgs<T> a) {
+    batch_query_wide<T, W, 32>(a);
 }
 
 // Launchers (batch_wide_f32.cu, batch_wide_f64.cu): W in {4, 6, 8}, G in {1, 32}.

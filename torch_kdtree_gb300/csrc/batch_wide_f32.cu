@@ -10,7 +10,9 @@ namespace tk {
 template <>
 const void* batch_wide_kernel<float>(int W, int G) {
 #define TK_BWPTR(w, g) \
-    if (W == w && G == g) return reinterpret_cast<const void*>(&k_batch_query_wide<float, w, g>);
+    if (W == w && G == g)                                                                \
+        return g == 1 ? reinterpret_cast<const void*>(&k_batch_query_wide1<float, w>)        \
+                      : reinterpret_cast<const void*>(&k_batch_query_wide32<float, w>);
     TK_BW_LIST(TK_BWPTR)
 #undef TK_BWPTR
     return nullptr;
@@ -21,7 +23,8 @@ int batch_wide_launch<float>(const WideBatchArgs<float>& a, int W, int G, int gr
     bool launched = false;
 #define TK_BWLAUNCH(w, g)                                        \
     if (!launched && W == w && G == g) {                         \
-        k_batch_query_wide<float, w, g><<<grid, 256, 0, s>>>(a);     \
+        if (g == 1) k_batch_query_wide1<float, w><<<grid, 256, 0, s>>>(a);                   \
+        else k_batch_query_wide32<float, w><<<grid, 256, 0, s>>>(a);                        \
         launched = true;                                         \
     }
     TK_BW_LIST(TK_BWLAUNCH)
