@@ -259,7 +259,9 @@ int tk_nn_distance(const void* ref, int64_t n, const void* q, int64_t nq, int di
  * (synchronise its stream first); pass the same shape arguments as that
  * call.  *flags: bit 0 = a bounded device-side wait of the tensor-core
  * kernel ran out, bit 1 = an input lay outside the tensor-core
- * certificate's range; *recomputed = queries the exact kernel recomputed.
+ * certificate's range; *recomputed = queries the exact kernel recomputed
+ * (all of them for k > 32 with dims > 32, where the candidate search's
+ * shared memory would not fit a block).
  * The answer is exact in every case: an unfinished or uncertifiable
  * candidate search only sends its queries to the exact kernel.  Returns
  * TK_ETIMEOUT when bit 0 is set, else TK_OK; TK_BRUTE_EXACT calls report

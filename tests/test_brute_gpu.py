@@ -123,6 +123,42 @@ def test_tensor_core_modes_are_exact(mode, d, k, oracle):
 
 
 @pytest.mark.parametrize("mode", ["tf32", "bf16_split"])
+@pytest.mark.parametrize("d", [3, 17, 40])
+@pytest.mark.parametrize("k", [33, 64])
+def test_tensor_core_large_k(mode, d, k, oracle):
+    """k above 32: the mma.sync candidate search with a 128-key over-fetch and
+    the two-register re-rank; d = 40 also leaves the tcgen05 path's depth."""
+    rng = np.random.default_rng(8800 + d + k)
+    ref = rng.standard_normal((30000, d)).astype(np.float32)
+    ref[rng.permutation(30000)[:500]] = ref[:500]  # exact duplicates
+    q = rng.standard_normal((700, d)).astype(np.float32)
+    dd, ii = tk().nn_distance(torch.from_numpy(ref).to(cuda), torch.from_numpy(q).to(cuda), k, mode=mode)
+    bd, bi = oracle.brute(ref, q, k)
+    np.testing.assert_array_equal(dd.cpu().numpy(), bd)
+    np.testing.assert_array_equal(ii.cpu().numpy(), bi)
+    if d == 40:  # too big for the candidate search's shared memory: every query exact
+        from torch_kdtree_gb300 import _lib
+        from torch_kdtree_gb300._lib import LIB
+        from torch_kdtree_gb300.nn_distance import _BRUTE_MODES, _stream_ptr
+        m = _BRUTE_MODES[mode]
+        r_t, q_t = torch.from_numpy(ref).to(cuda), torch.from_numpy(q).to(cuda)
+        wsb = LIB.tk_nn_distance_workspace_size(len(ref), len(q), d, k, _lib.TK_F32, m)
+        ws = torch.empty(wsb, dtype=torch.uint8, device=cuda)
+        d2 = torch.empty(len(q), k, device=cuda)
+        i2 = torch.empty(len(q), k, dtype=torch.int32, device=cuda)
+        _lib.check(LIB.tk_nn_distance(r_t.data_ptr(), len(ref), q_t.data_ptr(), len(q), d, k, _lib.TK_F32, m,
+                                      d2.data_ptr(), i2.data_ptr(), ws.data_ptr(), wsb, _stream_ptr(cuda)))
+        torch.cuda.synchronize()
+        import ctypes
+        flags, rec = ctypes.c_int(-1), ctypes.c_int(-1)
+        _lib.check(LIB.tk_nn_distance_report(ws.data_ptr(), len(ref), len(q), d, k, _lib.TK_F32, m,
+                                             ctypes.byref(flags), ctypes.byref(rec)))
+        assert flags.value == 0 and rec.value == len(q)
+        np.testing.assert_array_equal(d2.cpu().numpy(), bd)
+        np.testing.assert_array_equal(i2.cpu().numpy(), bi)
+
+
+@pytest.mark.parametrize("mode", ["tf32", "bf16_split"])
 @pytest.mark.parametrize("k", [8, 16, 32])
 @pytest.mark.parametrize("data", ["normal", "repeated", "grid"])
 def test_tensor_core_sampled_threshold_slices(mode, k, data, oracle):

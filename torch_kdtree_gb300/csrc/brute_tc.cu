@@ -109,6 +109,14 @@ TcWs tc_layout(int64_t n, int64_t nq, int d, int k, int mode, int sms) {
     return w;
 }
 
+// Every query on the fallback list: the tensor-core candidate search does
+// not fit this shape (see run_brute_tc), the exact kernel answers them all.
+__global__ void k_all_queries(int nq, int* list, int* count) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < nq) list[i] = i;
+    if (i == 0) *count = nq;
+}
+
 // Poll budget of the candidate kernel's bounded waits (0 = kT5MaxTries); set
 // by tk_set_device_wait_limit.
 std::atomic<uint32_t> g_wait_polls{0};
@@ -137,6 +145,25 @@ int run_brute_tc(const float* ref, int64_t n, const float* q, int64_t nq, int d,
     cudaError_t e0 = cudaMemsetAsync(p + w.err, 0, sizeof(int), s);
     int* err = reinterpret_cast<int*>(p + w.err);  // no certificates when set (see kTcNormLimit)
     if (e0 != cudaSuccess) return fail(TK_ECUDA, std::string("memset: ") + cudaGetErrorString(e0));
+    if (!w.tc5) {
+        // The mma.sync candidate search keeps 128 rows' lists and a score tile
+        // in shared memory; for k > 32 with d > 32 (C = 128, KP = 64) that is
+        // more than a block may have.  The answer is exact either way, so the
+        // exact kernel answers every query (tk_nn_distance_report: all
+        // recomputed) instead of failing the call.
+        int dev = 0, optin = 0;
+        cudaGetDevice(&dev);
+        if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) optin = 0;
+        if (select_smem_bytes(mode, w.KP, w.C) > size_t(optin)) {
+            int* list = reinterpret_cast<int*>(p + w.fail_list);
+            int* count = reinterpret_cast<int*>(p + w.fail_count);
+            k_all_queries<<<(nq32 + 255) / 256, 256, 0, s>>>(nq32, list, count);
+            const cudaError_t e1 = cudaGetLastError();
+            if (e1 != cudaSuccess) return fail(TK_ECUDA, std::string("fallback list: ") + cudaGetErrorString(e1));
+            return brute_fallback(ref, n, q, nq, d, k, dists, idx, list, count, p + w.brute,
+                                  brute_fallback_workspace_bytes(n, nq, d, k), s);
+        }
+    }
     int crc = TK_OK;
     if (w.tc5) {
         // 1-2. pack into the core-matrix layout and run the tcgen05 candidate kernel

@@ -764,12 +764,16 @@ __global__ void __launch_bounds__(kT5Threads, 1) k_tc5_select(const Tc5Args a) {
     if (warp == kT5EpiWarps) sm100::tmem_dealloc(tmem, 512);
 }
 
-template <int MODE, int KP, int C>
-size_t select_smem_bytes() {
-    constexpr int KW = (MODE == TK_BRUTE_TF32) ? KP : KP / 2;
-    constexpr int PLANES = (MODE == TK_BRUTE_TF32) ? 1 : 2;
+// Shared memory of the mma.sync candidate search for (mode, KP, C).
+inline size_t select_smem_bytes(int mode, int KP, int C) {
+    const int KW = (mode == TK_BRUTE_TF32) ? KP : KP / 2;
+    const int PLANES = (mode == TK_BRUTE_TF32) ? 1 : 2;
     return sizeof(uint32_t) * PLANES * kCols * (KW + 4) + sizeof(float) * kCols +
            sizeof(float) * kRows * (kCols + 4) + (sizeof(float) + sizeof(int32_t)) * size_t(C) * kRows;
+}
+template <int MODE, int KP, int C>
+size_t select_smem_bytes() {
+    return select_smem_bytes(MODE, KP, C);
 }
 
 struct RerankArgs {
