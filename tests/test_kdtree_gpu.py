@@ -370,3 +370,33 @@ def test_concurrent_queries_on_one_tree():
     assert not errors, errors
     for (wd, wi), (d, i) in zip(want, got):
         assert torch.equal(d, wd) and torch.equal(i, wi)
+
+
+def test_random_configurations(oracle):
+    """A seeded sweep over combinations the targeted tests take one at a time:
+    dims 1-8, float32 / float64, cloud and batch sizes from 1 up, any k <= n,
+    any depth, lanes per query, forced binning (cost-class order on small
+    batches), box pruning, traversal and shared-memory staging; every answer
+    bit-exact against the exhaustive search."""
+    rng = np.random.default_rng(20260)
+    for case in range(120):
+        dims = int(rng.integers(1, 9))
+        dtype = np.float32 if rng.random() < 0.7 else np.float64
+        n = int(rng.choice([2, 17, 300, 2500, 5000]))
+        nq = int(rng.choice([1, 3, 64, 700, 2000]))
+        k = int(rng.integers(1, min(n, 128) + 1))
+        levels = int(rng.integers(1, int(np.log2(n)) + 1))  # the build wants 2^levels <= n
+        tpq = int(rng.choice([0, 1, 4, 8, 32]))
+        opts = dict(threads_per_query=tpq, bin_queries=int(rng.choice([-1, 0, 1])),
+                    prune_boxes=int(rng.integers(0, 2)), traversal=int(rng.choice([0, 1, 2])),
+                    smem_levels=int(rng.choice([-1, 0, 4])))
+        scale = float(rng.choice([1e-3, 1.0, 1e3]))
+        ref = (rng.standard_normal((n, dims)) * scale).astype(dtype)
+        q = (rng.standard_normal((nq, dims)) * scale * 1.3).astype(dtype)
+        if n > 20:
+            ref[rng.integers(0, n, n // 10)] = ref[rng.integers(0, n, n // 10)]  # duplicates: ties
+        bd, bi = oracle.brute(ref, q, k)
+        d, i = gpu_query(ref, q, k, levels=levels, **opts)
+        msg = f"case {case}: dims={dims} {np.dtype(dtype).name} n={n} nq={nq} k={k} L={levels} {opts}"
+        np.testing.assert_array_equal(d, bd, err_msg=msg)
+        np.testing.assert_array_equal(i, bi, err_msg=msg)
