@@ -275,3 +275,26 @@ def test_infinite_and_huge_references(mode, oracle):
     assert bi[0, 0] == 11 and bd[0, 0] == 0
     np.testing.assert_array_equal(dd.cpu().numpy(), bd)
     np.testing.assert_array_equal(ii.cpu().numpy(), bi)
+
+
+def test_random_configurations(oracle):
+    """A seeded sweep over exhaustive-search shapes: dims 1-64, k up to 64 and
+    n, query counts from 1 up, every mode (tensor-core modes for float32),
+    duplicates; every answer bit-exact against the oracle."""
+    rng = np.random.default_rng(31337)
+    for case in range(60):
+        d = int(rng.choice([1, 2, 3, 5, 8, 12, 16, 24, 31, 32, 33, 39, 40, 47, 48, 64]))
+        n = int(rng.choice([1, 5, 64, 257, 1500, 4000]))
+        nq = int(rng.choice([1, 7, 129, 500]))
+        k = int(rng.integers(1, min(n, 64) + 1))
+        mode = str(rng.choice(["exact", "tf32", "bf16_split"]))
+        dtype = np.float64 if (mode == "exact" and rng.random() < 0.3) else np.float32
+        ref = (rng.standard_normal((n, d)) * float(rng.choice([1e-2, 1.0, 1e2]))).astype(dtype)
+        if n > 10:
+            ref[rng.integers(0, n, n // 8)] = ref[rng.integers(0, n, n // 8)]
+        q = rng.standard_normal((nq, d)).astype(dtype)
+        dd, ii = tk().nn_distance(torch.from_numpy(ref).to(cuda), torch.from_numpy(q).to(cuda), k, mode=mode)
+        bd, bi = oracle.brute(ref, q, k)
+        msg = f"case {case}: d={d} n={n} nq={nq} k={k} {mode} {np.dtype(dtype).name}"
+        np.testing.assert_array_equal(dd.cpu().numpy(), bd, err_msg=msg)
+        np.testing.assert_array_equal(ii.cpu().numpy(), bi, err_msg=msg)
