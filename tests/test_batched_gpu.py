@@ -93,3 +93,35 @@ def test_batch_of_wide_trees(dtype, dims, tpq, oracle):
         bd, bi = oracle.brute(r, q, k)
         np.testing.assert_array_equal(db.cpu().numpy(), bd)
         np.testing.assert_array_equal(ib.cpu().numpy(), bi)
+
+
+def test_random_batches(oracle):
+    """A seeded sweep of batches: 1-12 clouds of one dims (1-8) and dtype,
+    sizes from 2 up, per-cloud k and depth, empty query sets, every lane
+    shape; each cloud's answer bit-exact against the exhaustive search."""
+    from torch_kdtree_gb300.batched import BatchedKDTrees
+    rng = np.random.default_rng(4242)
+    for case in range(25):
+        dims = int(rng.integers(1, 9))
+        dtype = np.float32 if rng.random() < 0.75 else np.float64
+        nc = int(rng.integers(1, 13))
+        sizes = [int(rng.choice([2, 9, 150, 1200, 6000])) for _ in range(nc)]
+        nqs = [int(rng.choice([0, 1, 33, 400])) for _ in range(nc)]
+        tpq = int(rng.choice([0, 1, 8, 32]))
+        kmax = 16 if tpq == 1 else 128
+        ks = [int(rng.integers(1, min(n, kmax) + 1)) for n in sizes]
+        levels = [int(rng.integers(1, int(np.log2(n)) + 1)) if rng.random() < 0.7 else None for n in sizes]
+        refs_np = [rng.standard_normal((n, dims)).astype(dtype) for n in sizes]
+        qs_np = [rng.standard_normal((m, dims)).astype(dtype) for m in nqs]
+        if sum(nqs) == 0:
+            continue
+        b = BatchedKDTrees([torch.from_numpy(r).to(cuda) for r in refs_np], ks, nqs, levels=levels,
+                           threads_per_query=tpq)
+        d_b, i_b = b.query([torch.from_numpy(q).to(cuda) for q in qs_np])
+        for c, (r, q, k, db, ib) in enumerate(zip(refs_np, qs_np, ks, d_b, i_b)):
+            if len(q) == 0:
+                continue
+            bd, bi = oracle.brute(r, q, k)
+            msg = f"case {case} cloud {c}: dims={dims} {np.dtype(dtype).name} n={len(r)} k={k} tpq={tpq}"
+            np.testing.assert_array_equal(db.cpu().numpy(), bd, err_msg=msg)
+            np.testing.assert_array_equal(ib.cpu().numpy(), bi, err_msg=msg)
