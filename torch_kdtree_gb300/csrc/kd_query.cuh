@@ -506,21 +506,6 @@ __global__ void __launch_bounds__(256) k_kd_packet(const KdArgs<T> a) {
 
 // ---------------------------------------------------------- query binning --
 
-// Cost class of a query for the launch order (smaller = costlier).  The
-// squared distance from the query to the farthest corner of its home leaf's
-// bounding box bounds its distance to every point of that leaf, so it tracks
-// the radius the search must cover: queries far from their leaf's points
-// (outside the cloud, in sparse regions) scan many more leaves.  Its float
-// exponent and top mantissa bit give half-octave classes, 2^-63 .. 2^64
-// mapped onto 255 .. 0; an empty leaf or a non-finite value gets the last
-// class.
-__device__ __forceinline__ uint32_t cost_class(float far2) {
-    if (!(far2 <= 3.0e38f)) return 255u;
-    const uint32_t bucket = __float_as_uint(far2) >> 22;  // exponent and top mantissa bit
-    const uint32_t c = bucket < 128u ? 0u : (bucket - 128u > 255u ? 255u : bucket - 128u);
-    return 255u - c;
-}
-
 // Cell id at depth B of every query (same descent rule as the search), its
 // arrival rank within the cell, and (with `boxes`) its cost class from the
 // home leaf at depth L: bin_of = cell | class << 16 (B <= 16).

@@ -37,9 +37,9 @@ int kd_wide_launch<double>(const KdWideArgs<double>& a, int W, int G, int R, int
 }
 
 template <>
-void bin_count_wide_launch<double>(const double* q, int nq, int dims, const double* medians, int B, int* counts, int* bin_of,
-                                int* pos_of, cudaStream_t s) {
-    k_bin_count_wide<double><<<(nq + 255) / 256, 256, 0, s>>>(q, nq, dims, medians, B, counts, bin_of, pos_of);
+void bin_count_wide_launch<double>(const double* q, int nq, int dims, const double* medians, int B, int L, const double* boxes,
+                                int W, int* counts, int* bin_of, int* pos_of, cudaStream_t s) {
+    k_bin_count_wide<double><<<(nq + 255) / 256, 256, 0, s>>>(q, nq, dims, medians, B, L, boxes, W, counts, bin_of, pos_of);
 }
 
 }  // namespace tk

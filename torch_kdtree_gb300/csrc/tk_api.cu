@@ -310,8 +310,9 @@ int run_query_wide(const tk_tree* t, const T* q, int nq, int k, T* dists, int32_
 
     int* counter = nullptr;
     const int32_t* order = nullptr;
-    const int rc0 = prepare_order(t, nq, o, ws, s, &counter, &order, false, [&](int B, int* counts, int* bin_of, int* pos_of) {
-        bin_count_wide_launch<T>(q, nq, t->dims, static_cast<const T*>(t->d_medians), B, counts, bin_of, pos_of, s);
+    const int rc0 = prepare_order(t, nq, o, ws, s, &counter, &order, true, [&](int B, int* counts, int* bin_of, int* pos_of) {
+        bin_count_wide_launch<T>(q, nq, t->dims, static_cast<const T*>(t->d_medians), B, L,
+                                 static_cast<const T*>(t->d_boxes), W, counts, bin_of, pos_of, s);
     });
     if (rc0 != TK_OK) return rc0;
 
