@@ -245,9 +245,10 @@ def test_wide_trees_every_shape(dims, dtype, oracle):
     for k in (1, 5, 16, 17, 100):
         bd, bi = oracle.brute(ref, q, k)
         for levels in (1, 5, 9):
-            for tpq, boxes in ((0, 1), (1, 1), (1, 0), (32, 1), (8, 0)):
-                d, i = gpu_query(ref, q, k, levels=levels, threads_per_query=tpq, prune_boxes=boxes)
-                np.testing.assert_array_equal(d, bd, err_msg=f"k={k} L={levels} tpq={tpq} boxes={boxes}")
+            # binq=1 forces the cell + cost-class launch order on this small batch
+            for tpq, boxes, binq in ((0, 1, -1), (1, 1, 1), (1, 0, -1), (32, 1, 1), (8, 0, -1), (32, 0, 1)):
+                d, i = gpu_query(ref, q, k, levels=levels, threads_per_query=tpq, prune_boxes=boxes, bin_queries=binq)
+                np.testing.assert_array_equal(d, bd, err_msg=f"k={k} L={levels} tpq={tpq} boxes={boxes} binq={binq}")
                 np.testing.assert_array_equal(i, bi)
 
 
