@@ -694,7 +694,10 @@ def row_batched(dev, steps, warmup, flush, threads):
             "batched_vs_plain": ms_plain / ms_batch, "identical_results_batched_vs_plain": same,
             "roofline": {"bound": "hbm", "achieved": alg / (ms_batch / 1e3) / 1e9, "peak": peak, "peak_kind": kind,
                          "unit": "GB/s", "frac": alg / (ms_batch / 1e3) / 1e9 / peak,
-                         "algorithmic_bytes_per_launch": alg},
+                         "algorithmic_bytes_per_launch": alg, "kernel": "k_batch_query",
+                         "traffic": profiled_traffic("batch_query_256_ragged"),
+                         "traffic_profile": "profiles/batch_query_256_ragged.md"
+                         if profiled_traffic("batch_query_256_ragged") is not None else None},
             "exactness_vs_oracle": {"clouds": len(pick), "queries": int(sum(c.n_queries for c in checks)),
                                     "index_mismatches_non_tie": int(sum(c.mismatches for c in checks)),
                                     "tie_queries": int(sum(c.tie_queries for c in checks)),
@@ -803,6 +806,11 @@ def run_batched(args):
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
     leaf = args.leaf_size
     tuned_levels = [int(max(1, min(24, round(np.log2(max(2, len(r)) / leaf))))) for r, _, _ in clouds]
+    if args.profile:  # the tuned batch once (trees built on the host: few launches before the batched kernel)
+        b = BatchedKDTrees([torch.from_numpy(r) for r, _, _ in clouds], ks, qc, levels=tuned_levels, device=dev)
+        b.graph(q_flat)()
+        torch.cuda.synchronize()
+        return
     t0 = time.perf_counter()
     plain = BatchedKDTrees(refs, ks, qc)  # reference heuristic depth per cloud
     tuned = BatchedKDTrees(refs, ks, qc, levels=tuned_levels)
