@@ -22,6 +22,9 @@ def test_roofline_inputs_come_from_the_committed_profile():
     assert isinstance(traffic, int) and traffic > 100_000_000
     assert isinstance(inst, int) and inst > 1_000_000_000
     assert b.profiled_traffic("no_such_profile") is None
+    # the batched row's DRAM traffic: one launch over the 256 ragged clouds
+    batch = b.profiled_traffic("batch_query_256_ragged")
+    assert isinstance(batch, int) and 400_000_000 < batch < 2_000_000_000
 
 
 def test_algorithmic_bytes_of_the_headline_launch():
