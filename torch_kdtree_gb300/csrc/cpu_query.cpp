@@ -13,9 +13,10 @@
 // distance; children are taken near side first (the reference's rule,
 // src/kdtree.cpp:30).  Boxes that only tie the k-th distance are still
 // entered, so the result equals an exhaustive search ordered by
-// (distance, original index).  Queries are split into contiguous blocks over
-// host threads.
+// (distance, original index).  Queries are searched in tree-cell order by
+// host threads pulling chunks of that order.
 #include <algorithm>
+#include <atomic>
 #include <cstdint>
 #include <limits>
 #include <thread>
@@ -111,26 +112,58 @@ struct CpuSearch {
     }
 };
 
+// Cell of a query at depth B (the search's descent rule), for the order below.
 template <typename T, int D>
-void search_block(const HostTree<T>& h, const T* q, int64_t b, int64_t e, int k, T* dists, int32_t* idx) {
-    CpuSearch<T, D> s(h, k);
-    for (int64_t i = b; i < e; ++i) s.run(q + i * D, dists + i * k, idx + i * k);
+uint32_t home_cell(const HostTree<T>& h, const T* q, int B) {
+    int node = 0;
+    for (int depth = 0; depth < B; ++depth) node = 2 * node + (q[depth % D] < h.medians[node] ? 1 : 2);
+    return uint32_t(node - ((1 << B) - 1));
 }
 
 template <typename T, int D>
 void search_all(const HostTree<T>& h, const T* q, int64_t nq, int k, T* dists, int32_t* idx, int n_threads) {
     int nt = n_threads > 0 ? n_threads : int(std::max(1u, std::thread::hardware_concurrency()));
     nt = int(std::min<int64_t>(nt, std::max<int64_t>(1, nq / 64)));
+    // Queries are taken in the order of the tree cell they fall into (a
+    // counting sort over the cells at depth B), so consecutive searches of a
+    // thread walk nearly the same nodes and leaves while they are in cache;
+    // threads pull chunks of that order from a shared counter.
+    int B = 0;
+    while (B < h.levels && B < 16 && (int64_t(1) << (B + 6)) <= nq) ++B;
+    std::vector<int32_t> order;
+    if (B > 0) {
+        const size_t ncell = size_t(1) << B;
+        std::vector<uint32_t> cell(static_cast<size_t>(nq));
+        std::vector<int64_t> start(ncell + 1, 0);
+        for (int64_t i = 0; i < nq; ++i) {
+            cell[size_t(i)] = home_cell<T, D>(h, q + i * D, B);
+            ++start[cell[size_t(i)] + 1];
+        }
+        for (size_t c = 0; c < ncell; ++c) start[c + 1] += start[c];
+        order.resize(size_t(nq));
+        for (int64_t i = 0; i < nq; ++i) order[size_t(start[cell[size_t(i)]]++)] = int32_t(i);
+    }
+    const int64_t chunk = 256;
+    std::atomic<int64_t> next{0};
+    auto work = [&]() {
+        CpuSearch<T, D> s(h, k);
+        for (;;) {
+            const int64_t b = next.fetch_add(chunk);
+            if (b >= nq) break;
+            const int64_t e = std::min(nq, b + chunk);
+            for (int64_t t = b; t < e; ++t) {
+                const int64_t i = order.empty() ? t : order[size_t(t)];
+                s.run(q + i * D, dists + i * k, idx + i * k);
+            }
+        }
+    };
     if (nt <= 1) {
-        search_block<T, D>(h, q, 0, nq, k, dists, idx);
+        work();
         return;
     }
     std::vector<std::thread> pool;
     pool.reserve(nt);
-    for (int t = 0; t < nt; ++t) {
-        const int64_t b = nq * t / nt, e = nq * (t + 1) / nt;
-        pool.emplace_back(search_block<T, D>, std::cref(h), q, b, e, k, dists, idx);
-    }
+    for (int t = 0; t < nt; ++t) pool.emplace_back(work);
     for (auto& th : pool) th.join();
 }
 
