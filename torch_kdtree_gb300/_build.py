@@ -57,7 +57,9 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
                    "-Xcompiler", "-ffp-contract=off", "--expt-relaxed-constexpr",
                    "-I", os.path.join(ROOT, "include"), "-c", src, "-o", obj]
         else:
-            cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-pthread",
+            # -O3 vectorises the CPU search's distance loops; without -ffast-math
+            # every lane rounds each operation as the scalar code does
+            cmd = ["g++", "-O3", "-std=c++17", "-fPIC", "-ffp-contract=off", "-pthread",
                    "-I", os.path.join(ROOT, "include"), "-c", src, "-o", obj]
         cmds.append(cmd)
 

@@ -39,6 +39,8 @@ struct CpuSearch {
     std::vector<T> ld;         // the k best distances, ascending
     std::vector<uint32_t> li;  // their original indices
     std::vector<int> stack;
+    static constexpr int kChunk = 64;
+    T dist[kChunk];
 
     CpuSearch(const HostTree<T>& tree, int kk) : h(tree), k(kk), ld(kk), li(kk) {
         stack.reserve(2 * kMaxLevels + 2);
@@ -86,15 +88,24 @@ struct CpuSearch {
                 if (node >= first_leaf) {
                     const int leaf = node - first_leaf;
                     const int beg = h.leaf_off[leaf], end = h.leaf_off[leaf + 1];
-                    for (int j = beg; j < end; ++j) {
-                        const T* p = h.structured.data() + size_t(j) * D;
-                        T acc = T(0);
-                        for (int c = 0; c < D; ++c) {
-                            const T dc = T(q[c] - p[c]);
-                            const T sq = T(dc * dc);
-                            acc = c == 0 ? sq : T(acc + sq);
+                    // distances of a chunk of the leaf first (a loop without
+                    // branches, which the compiler vectorises), then the offers
+                    for (int j0 = beg; j0 < end; j0 += kChunk) {
+                        const int m = std::min(kChunk, end - j0);
+                        const T* p = h.structured.data() + size_t(j0) * D;
+                        for (int j = 0; j < m; ++j) {
+                            const T* pj = p + size_t(j) * D;
+                            const T d0 = T(q[0] - pj[0]);
+                            T acc = T(d0 * d0);
+                            for (int c = 1; c < D; ++c) {
+                                const T dc = T(q[c] - pj[c]);
+                                acc = T(acc + T(dc * dc));
+                            }
+                            dist[j] = acc;
                         }
-                        offer(acc, uint32_t(h.perm[j]));
+                        const T worst = ld[k - 1];
+                        for (int j = 0; j < m; ++j)
+                            if (dist[j] <= worst) offer(dist[j], uint32_t(h.perm[j0 + j]));
                     }
                     continue;
                 }
