@@ -1081,6 +1081,55 @@ def run_wide(args):
     print(json.dumps(line), flush=True)
 
 
+def run_cpu_tree(args):
+    """CPU trees (build_kd_tree(..., device="cpu"), the reference's KDTreeCPU
+    path): the library's threaded host search against the reference's CPU
+    search (oracle restatement, same threads) on 131,072 queries of the large
+    single-cloud workload (4,194,304 refs, k=16), at the reference's default
+    depth and at depth 18; exactness against the oracle's answers."""
+    import torch
+
+    import torch_kdtree_gb300 as tk
+    from oracle import oracle as O
+    from torch_kdtree_gb300.synthetic import cube_and_sphere
+    O.build()
+    ref_np, q_all = cube_and_sphere()[:2]
+    nq, k = 131072, 16
+    q_np = np.ascontiguousarray(q_all[:nq])
+    threads = os.cpu_count() or 1
+    qt = torch.from_numpy(q_np)
+    runs = {}
+    for levels in (O.default_levels(len(ref_np)), 18):
+        tree = tk.build_kd_tree(torch.from_numpy(ref_np), device="cpu", levels=levels)
+        lay = O.build_tree(ref_np, levels, nthreads=threads)
+        ours = ora = 1e30
+        tree.query(qt[:4096], nr_nns_searches=k)  # warm-up: host threads started, pages touched
+        O.query_tree(lay, q_np[:4096], k, nthreads=threads)
+        for _ in range(3):
+            t0 = time.perf_counter()
+            d, i = tree.query(qt, nr_nns_searches=k)
+            ours = min(ours, time.perf_counter() - t0)
+            t0 = time.perf_counter()
+            od, oi = O.query_tree(lay, q_np, k, nthreads=threads)
+            ora = min(ora, time.perf_counter() - t0)
+        cmp = O.compare_knn(od, oi, d.numpy(), i.numpy())
+        runs[f"levels{levels}"] = {"queries_per_s": nq / ours, "reference_cpu_queries_per_s": nq / ora,
+                                   "speedup": ora / ours,
+                                   "exact_vs_reference_cpu": {"index_mismatches_non_tie": cmp.mismatches,
+                                                              "tie_queries": cmp.tie_queries,
+                                                              "dist_bit_mismatches": cmp.dist_bit_mismatch}}
+    key = f"levels{O.default_levels(len(ref_np))}"
+    line = {
+        "metric": "KNN queries/s of CPU trees (host search), 4,194,304 refs, k=16; value = the reference's default depth",
+        "value": runs[key]["queries_per_s"], "unit": UNIT, "n_gpus": 0, "steps": 3,
+        "higher_is_better": True, "dtype": "f32", "data": "synthetic (seeded numpy)",
+        "config": {"workload": f"CPU tree query, {nq} of the large single-cloud queries, best of 3 calls",
+                   "host_threads": threads},
+        "runs": runs,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_brute_tc(args):
     """Tensor-core brute force vs the FP32 CUDA-core brute force: 262,144 refs,
     65,536 queries, N(0,1) in d = 8 and 32 with 5% exact duplicate refs, k=32.
@@ -1155,7 +1204,7 @@ def main():
                    help="chosen: 1 = per-query stacks, 2 = warp packets (with --levels/--tpq)")
     p.add_argument("--profile", action="store_true", help="run one chosen and one plain query only (for ncu)")
     p.add_argument("--workload", default="kd",
-                   choices=["kd", "plain", "readme", "batched", "backward", "brute", "brute_tc", "wide"],
+                   choices=["kd", "plain", "readme", "batched", "backward", "brute", "brute_tc", "wide", "cpu_tree"],
                    help="kd (default): the headline large single-cloud query; the others measure the "
                         "batched, backward and brute-force paths")
     p.add_argument("--leaf-size", type=int, default=16, help="target points per leaf of tuned batch trees")
@@ -1171,7 +1220,7 @@ def main():
         if rank == 0:
             {"plain": run_plain, "readme": run_readme, "batched": run_batched, "backward": run_backward,
              "brute": run_brute,
-             "brute_tc": run_brute_tc, "wide": run_wide}[args.workload](args)
+             "brute_tc": run_brute_tc, "wide": run_wide, "cpu_tree": run_cpu_tree}[args.workload](args)
         return
     if world > 1:
         import torch
