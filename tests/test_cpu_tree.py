@@ -122,3 +122,27 @@ def test_cpu_query_rejects_a_null_tree():
     q = np.zeros((1, 3), np.float32)
     assert LIB.tk_tree_query_cpu(None, q.ctypes.data, 1, 1, d.ctypes.data, i.ctypes.data, 0) == TK_EINVAL
     assert b"null" in LIB.tk_last_error()
+
+
+def test_cpu_query_order_and_threads_do_not_change_answers(oracle):
+    """The host search takes queries in tree-cell order (from 128 queries on)
+    in 256-query chunks pulled by the threads: every batch size around those
+    boundaries and every thread count gives the exhaustive search's answer."""
+    import ctypes
+    from torch_kdtree_gb300._lib import LIB
+    rng = np.random.default_rng(11)
+    ref = rng.standard_normal((2000, 3)).astype(np.float32)
+    ref[50:80] = ref[:30]  # exact duplicates: ties
+    q_all = (rng.standard_normal((4099, 3)) * 1.3).astype(np.float32)
+    k = 9
+    tree = tk().build_kd_tree(torch.from_numpy(ref), device="cpu", levels=6)
+    h = tree._tree.handle
+    for nq in (1, 63, 127, 128, 129, 255, 257, 1000, 4099):
+        q = np.ascontiguousarray(q_all[:nq])
+        bd, bi = oracle.brute(ref, q, k)
+        for threads in (1, 3, 16):
+            d = np.empty((nq, k), np.float32)
+            i = np.empty((nq, k), np.int32)
+            assert LIB.tk_tree_query_cpu(h, q.ctypes.data, nq, k, d.ctypes.data, i.ctypes.data, threads) == 0
+            np.testing.assert_array_equal(d, bd, err_msg=f"nq={nq} threads={threads}")
+            np.testing.assert_array_equal(i, bi, err_msg=f"nq={nq} threads={threads}")
